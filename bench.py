@@ -1,0 +1,390 @@
+"""Benchmark of the per-frame hot path: path segments per second.
+
+Workload (default, `icosphere1080p`): displaced icosphere, subdivision level 8 (1,310,720 triangles,
+radius 1, per-vertex normal displacement N(0, 0.02)) in a 10^3 Lambertian room, seeded per-triangle
+materials (60% Lambertian, 25% GGX metal, 15% dielectric), 1024^2 rgba8 albedo / MR / normal value-noise
+textures, one 1x1 area light (emission 20) and 4 seeded point lights; 1920x1080, 4 spp per frame,
+depth 8, NEE on, no photon map, no denoise; accumulation over 32 frames.  A step is one progressive
+frame (gather, then composite + tonemap).  Synthetic, seeded inputs; the scene (~330 MB on the device)
+is larger than L2, so no L2 flush is needed between steps.
+
+Metric: segments/s, a segment being one closest-hit BVH trace on a camera or bounce path (shadow
+rays are reported separately).  `value` is device-timed with CUDA events on the renderer's stream;
+`e2e` is the same metric through the public API with host buffers (camera in, rgba8 frame out into
+pinned memory) timed on the host clock.
+
+`--impl reference` times the reference's CPU restatement (the oracle: the Rust/WGSL reference needs
+wgpu and a graphics stack, which this machine does not have) on the host cores, on bounded samples
+(row bands) of the same frames.
+
+Launch: python bench.py [--gpus N --steps K --warmup W] ; N > 1 under torch.distributed.run, one
+independent render job per GPU (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "icosphere1080p": dict(scene="icosphere", level=8, seed=0, sigma=0.02, tex=1024, width=1920, height=1080, spp=4,
+                           max_bounces=8, accumulate_frames=32, denoise=False, photons=0),
+    "cornell256": dict(scene="cornell", width=256, height=256, spp=1, max_bounces=6, accumulate_frames=16,
+                       denoise=False, photons=0),
+}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def hbm_peak() -> tuple[float, str]:
+    pk = measured_peaks()
+    if "hbm_gbs" in pk:
+        return float(pk["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(w: dict):
+    import rustracer_gb300 as rt
+
+    if w["scene"] == "cornell":
+        return rt.Scene.cornell555()
+    return rt.Scene.icosphere_room(w["level"], w["seed"], w["sigma"], w["tex"])
+
+
+def make_config(w: dict):
+    import rustracer_gb300 as rt
+
+    return rt.RenderConfig(width=w["width"], height=w["height"], spp=w["spp"], accumulate_frames=w["accumulate_frames"],
+                           enable_denoise=w["denoise"], enable_photon_map=bool(w["photons"]),
+                           photon_count=max(w["photons"], 1), max_bounces=w["max_bounces"])
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU legs (oracle): bounded samples of the same frames
+# ------------------------------------------------------------------------------------------------
+def cpu_sample(scene, cfg, cam, seconds: float, threads: int, frames: int = 1):
+    """Times the oracle on row bands of `frames` consecutive frames, sized to ~`seconds` in total.
+    Returns (segments/s, sample description, per-ray work counters)."""
+    import oracle
+
+    u = oracle.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, cfg.width, cfg.height, cam.near,
+                              cam.aperture, cam.focus_dist)
+    o = oracle.OracleRenderer(scene.describe(), cfg, u, threads=threads)
+    # calibrate on a small band
+    rows = max(1, min(cfg.height, 4 * max(threads, 1)))
+    t0 = time.perf_counter()
+    o.sample_counter = 0
+    _gather_rows(o, (cfg.height // 2 - rows // 2, cfg.height // 2 - rows // 2 + rows))
+    dt = time.perf_counter() - t0
+    per_row = dt / rows
+    band = int(max(1, min(cfg.height, seconds / max(per_row, 1e-6) / max(frames, 1))))
+    y0 = max(0, cfg.height // 2 - band // 2)
+    o.counters[:] = 0
+    t0 = time.perf_counter()
+    for f in range(frames):
+        _gather_rows(o, (y0, y0 + band))
+    dt = time.perf_counter() - t0
+    c = o.counters.astype(np.float64)
+    seg = c[0]
+    desc = (f"rows {y0}..{y0 + band} of {frames} frame(s) of {cfg.width}x{cfg.height}, spp {cfg.spp}, "
+            f"depth {cfg.max_bounces or 6} ({int(seg)} segments in {dt:.1f} s)")
+    rays = max(c[0] + c[1], 1.0)
+    work = {"nodes_per_ray": c[2] / rays, "tris_per_ray": c[3] / rays, "hit_fraction": c[4] / max(c[0], 1.0),
+            "shadow_per_segment": c[1] / max(c[0], 1.0)}
+    return seg / dt, desc, work
+
+
+def _gather_rows(o, rows):
+    """One gather dispatch of the oracle over a row band (the CPU cost of the frame)."""
+    import ctypes as C
+
+    import oracle
+
+    o.sample_counter += 1
+    o.frames_since_reset += 1
+    ip = o.image_params(o.alpha())
+    mb = o.cfg.max_bounces or 6
+    oracle.load().oracle_gather(C.cast(C.pointer(o.desc), C.c_void_p), C.byref(o.cam), C.byref(ip), mb,
+                                C.byref(o.gp), None, len(o.sorted), None, rows[0], rows[1], o.threads,
+                                oracle._p(o.frame), oracle._p(o.moments), oracle._p(o.gbuffer), oracle._p(o.counters))
+
+
+def run_reference(args, w):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    scene = make_scene(w)
+    cfg = make_config(w)
+    cam = scene.default_camera()
+    # warm-up samples, then K timed samples (one row band each)
+    per_step = max(1.0, min(20.0, 120.0 / max(args.steps + args.warmup, 1)))
+    for _ in range(args.warmup):
+        cpu_sample(scene, cfg, cam, per_step / 4, threads)
+    vals, descs = [], []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, d, _ = cpu_sample(scene, cfg, cam, per_step, threads)
+        vals.append(v)
+        descs.append(d)
+    wall = time.perf_counter() - t_all
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, **{k: v for k, v in w.items()}, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
+                             "sample": descs[0]},
+            "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference = the oracle's C++ restatement of the WGSL path on the host cores; the Rust/wgpu "
+                    "reference cannot run here (no Rust toolchain, no graphics stack)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+def load_traffic(workload: str) -> float | None:
+    """DRAM bytes per gather launch from the committed ncu summary of this workload, if present."""
+    p = ROOT / "profiles" / f"gather_{workload}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, w):
+    import torch
+
+    import rustracer_gb300 as rt
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = dist_mod
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    scene = make_scene(w)
+    cfg = make_config(w)
+    cam = scene.default_camera()
+    if rank:
+        cam.orbit(0.1 * rank, 0.0)  # an independent job per rank
+    r = rt.Renderer(scene, cfg)
+    r.update_camera(cam)
+    stream = torch.cuda.ExternalStream(r.stream())
+
+    for _ in range(args.warmup):
+        r.record_frame()
+    r.synchronize()
+    s0 = r.stats()  # drains the warm-up timings
+
+    # ---- device-timed region ----------------------------------------------------------------
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r.record_frame()
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    s1 = r.stats()
+    segments = s1.segments - s0.segments
+    shadow = s1.shadow_rays - s0.shadow_rays
+
+    t = torch.tensor([ms, float(segments), float(shadow)], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms_max = float(tmax[0])
+    else:
+        ms_max = float(t[0])
+    seg_all, shd_all = float(t[1]), float(t[2])
+    value = seg_all / (ms_max / 1000.0)
+
+    # ---- end-to-end through the public API with host buffers --------------------------------
+    out = torch.empty((cfg.height, cfg.width, 4), dtype=torch.uint8, pin_memory=True)
+    out_np = out.numpy()
+    s_e0 = r.stats()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.update_camera(cam)
+        r.record_frame()
+        r.read_tonemapped(out_np)
+    t1 = time.perf_counter()
+    s_e1 = r.stats()
+    e2e_seg = float(s_e1.segments - s_e0.segments)
+    e2e_t = torch.tensor([t1 - t0, e2e_seg], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        e_max = e2e_t.clone()
+        dist.all_reduce(e_max, op=dist.ReduceOp.MAX)
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.SUM)
+        e2e_wall = float(e_max[0])
+    else:
+        e2e_wall = float(e2e_t[0])
+    e2e_value = float(e2e_t[1]) / e2e_wall
+
+    if rank == 0:
+        gather_ms = s1.ms_gather_sum / max(s1.timed_frames, 1)
+        resolve_ms = s1.ms_resolve_sum / max(s1.timed_frames, 1)
+        # CPU baseline (oracle on this host's cores, bounded sample) and the per-ray work it counts.
+        threads = os.cpu_count() or 1
+        cpu_val, cpu_desc, work = cpu_sample(scene, cfg, cam, args.cpu_seconds, threads)
+        seg_per_frame = segments / max(args.steps, 1)
+        shd_per_frame = shadow / max(args.steps, 1)
+        rays = seg_per_frame + shd_per_frame
+        # Algorithmic bytes of one gather launch: 48 B per node fetch, 4 + 48 B per triangle test
+        # (prim index + vertices), 128 + 64 B of triangle + material per hit, 48 B of frame outputs
+        # per pixel.
+        algo = (rays * (48.0 * work["nodes_per_ray"] + 52.0 * work["tris_per_ray"])
+                + 192.0 * seg_per_frame * work["hit_fraction"] + 48.0 * cfg.width * cfg.height)
+        peak, peak_kind = hbm_peak()
+        achieved = algo / (gather_ms / 1000.0) / 1e9
+        traffic = load_traffic(args.workload)
+        line = {
+            "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, **{k: v for k, v in w.items()}, "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "shadow_rays_per_s": shd_all / (ms_max / 1000.0),
+            "gpu_launches": int(2 * args.steps),
+            "kernel_ms": {"gather": gather_ms, "resolve": resolve_ms},
+            "roofline": {"bound": "hbm", "kernel": "gather_kernel", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6.8 TB/s",
+                         "algorithmic_bytes_per_launch": algo,
+                         "work_per_ray": work},
+            "cpu_baseline": {"value": cpu_val, "unit": "segments/s", "cores": threads, "kind": "port",
+                             "sample": cpu_desc},
+            "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": 96 + 80,
+                    "d2h_bytes_per_step": int(cfg.width * cfg.height * 4)},
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    r.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="icosphere1080p")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="size of the CPU-baseline sample")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_ours(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

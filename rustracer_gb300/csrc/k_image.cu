@@ -1,0 +1,125 @@
+// Image-space kernels of the frame: the edge-aware a-trous denoise pass and the fused resolve
+// (composite into the accumulation history, then exposure / Reinhard / gamma into rgba8).
+//
+//   denoise  rustracer-renderer/shaders/denoise.wgsl:122-195  (HBM-bound stencil: 64 B/px compulsory)
+//   resolve  rustracer-renderer/shaders/composite.wgsl:211-221 + tonemap.wgsl:240-271
+//            (streaming: frame 16 B + history 16 B read, history 16 B + rgba8 4 B written per pixel)
+#include "rt_kernels.h"
+
+namespace rtd {
+
+__device__ __forceinline__ float luminance(f3 c) { return dot(c, mk3(0.2126f, 0.7152f, 0.0722f)); }
+
+// One a-trous pass, one thread per pixel.  The 3x3 moment window and the 5x5 tap window are served
+// from L1/L2: each input pixel is fetched from HBM once per pass.
+__global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__ in, float4 *__restrict__ out,
+                                                      const float4 *__restrict__ gbuffer,
+                                                      const float4 *__restrict__ moments,
+                                                      const rt_denoise_params p) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t W = p.width, H = p.height;
+    if (x >= W || y >= H) return;
+    const int32_t step = (int32_t)p.step_size;
+    const size_t idx = (size_t)y * W + x;
+    const f3 center = xyz(__ldg(in + idx));
+    const float4 gc = __ldg(gbuffer + idx);
+    const f3 n_center = xyz(gc);
+    const float d_center = gc.w;
+    const float lum_center = luminance(center);
+
+    float var_acc = 0.0f, var_cnt = 0.0f;
+    for (int32_t qy = -1; qy <= 1; ++qy)
+        for (int32_t qx = -1; qx <= 1; ++qx) {
+            int32_t nx = (int32_t)x + qx, ny = (int32_t)y + qy;
+            if (nx < 0 || ny < 0 || nx >= (int32_t)W || ny >= (int32_t)H) continue;
+            float2 m = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)ny * W + nx));
+            var_acc += fmaxf(m.y - m.x * m.x, 0.0f);
+            var_cnt += 1.0f;
+        }
+    const float var_frame = var_acc / fmaxf(var_cnt, 1.0f);
+    const float ema_scale = p.alpha / fmaxf(2.0f - p.alpha, 1e-4f);
+    const float var_c = var_frame * ema_scale;
+    const float denom_c = var_c * p.lambda + 1e-6f;
+    const float denom_d = p.phi_depth * fmaxf(d_center, 1e-4f);
+    const float k1d[3] = {0.375f, 0.25f, 0.0625f};
+
+    f3 sum = mk3(0.0f, 0.0f, 0.0f);
+    float total = 0.0f;
+#pragma unroll
+    for (int32_t dy = -2; dy <= 2; ++dy) {
+#pragma unroll
+        for (int32_t dx = -2; dx <= 2; ++dx) {
+            int32_t nx = (int32_t)x + dx * step, ny = (int32_t)y + dy * step;
+            if (nx < 0 || ny < 0 || nx >= (int32_t)W || ny >= (int32_t)H) continue;
+            size_t q = (size_t)ny * W + nx;
+            f3 nb = xyz(__ldg(in + q));
+            float4 g = __ldg(gbuffer + q);
+            float sw = k1d[dx < 0 ? -dx : dx] * k1d[dy < 0 ? -dy : dy];
+            float nw = powf(fmaxf(dot(n_center, xyz(g)), 0.0f), p.phi_normal);
+            float dw = expf(-fabsf(d_center - g.w) / denom_d);
+            float dl = luminance(nb) - lum_center;
+            float cw = expf(-(dl * dl) / denom_c);
+            float w = sw * nw * dw * cw;
+            sum = sum + nb * w;
+            total += w;
+        }
+    }
+    f3 o = total > 1e-6f ? sum / total : center;
+    out[idx] = make_float4(o.x, o.y, o.z, 1.0f);
+}
+
+cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
+                           const rt_denoise_params &p, cudaStream_t st) {
+    dim3 block(32, 8);
+    dim3 grid((p.width + block.x - 1) / block.x, (p.height + block.y - 1) / block.y);
+    denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    return cudaGetLastError();
+}
+
+// composite.wgsl mix() then tonemap.wgsl, one pixel per thread, 1-D over the image.
+__global__ void __launch_bounds__(256) resolve_kernel(const float4 *__restrict__ frame, float4 *__restrict__ accum,
+                                                      const float4 *__restrict__ gbuffer, uint32_t width,
+                                                      uint32_t npix, float alpha, const rt_tonemap_params tp,
+                                                      uchar4 *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    const float4 f = __ldg(frame + i);
+    const float4 a = accum[i];
+    const float om = 1.0f - alpha;
+    const float4 h = make_float4(a.x * om + f.x * alpha, a.y * om + f.y * alpha, a.z * om + f.z * alpha,
+                                 a.w * om + f.w * alpha);
+    accum[i] = h;
+    const f3 exposed = mk3(h.x, h.y, h.z) * tp.exposure;
+    const f3 mapped = exposed / (exposed + mk3(1.0f, 1.0f, 1.0f));
+    const float ig = 1.0f / tp.gamma;
+    f3 color = mk3(powf(mapped.x, ig), powf(mapped.y, ig), powf(mapped.z, ig));
+    if (tp.marker[3] > 0.0f) {
+        const uint32_t x = i % width, y = i / width;
+        float ddx = ((float)x + 0.5f) - tp.marker[0], ddy = ((float)y + 0.5f) - tp.marker[1];
+        float d = sqrtf(ddx * ddx + ddy * ddy);
+        float r = fmaxf(tp.marker[2], 1.5f);
+        float hit_dist = gbuffer ? __ldg(gbuffer + i).w : 1e30f;
+        if (hit_dist > tp.marker[3] - 0.2f) {
+            float ball = 1.0f - smoothstepf(r * 0.75f, r, d);
+            float halo = 1.0f - smoothstepf(r, r * 3.5f, d);
+            f3 core = mk3(1.0f, 0.94f, 0.80f) * powf(ball, 1.4f) * 0.85f;
+            f3 ring = mk3(1.0f, 0.46f, 0.14f) * halo * halo * 0.8f;
+            color = color + (core + ring) * tp.glow * (mk3(1.0f, 1.0f, 1.0f) - 0.55f * color);
+        }
+    }
+    auto q8 = [](float c) -> unsigned char {
+        return (unsigned char)__float2uint_rz(clampf(c, 0.0f, 1.0f) * 255.0f + 0.5f);
+    };
+    out[i] = make_uchar4(q8(color.x), q8(color.y), q8(color.z), 255);
+}
+
+cudaError_t launch_resolve(const float4 *frame, float4 *accum, const float4 *gbuffer, uint32_t width,
+                           uint32_t height, float alpha, const rt_tonemap_params &tp, uchar4 *out, cudaStream_t st) {
+    const uint32_t npix = width * height;
+    const uint32_t block = 256;
+    resolve_kernel<<<(npix + block - 1) / block, block, 0, st>>>(frame, accum, gbuffer, width, npix, alpha, tp, out);
+    return cudaGetLastError();
+}
+
+}  // namespace rtd

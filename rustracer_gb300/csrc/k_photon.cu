@@ -1,0 +1,493 @@
+// Photon pass of rebuild_photons (rustracer-renderer/src/lib.rs:913-1037):
+//
+//   photon_trace_kernel   photon_trace.wgsl:101-260.  Also emits the u32 cell key of every slot it
+//                         stores (photon_count.wgsl:18-32), so the grid build never re-reads positions.
+//   photon_keys_kernel    keys of a photon buffer loaded from the host (same key function).
+//   grid build            exact u32 counting sort of the slots by cell key:
+//     count_kernel        histogram (photon_count.wgsl:25-34), warp-aggregated atomics
+//     scan_*              device exclusive scan of the counts into (start, count) pairs; replaces the
+//                         blocking read-back and host scan of lib.rs:956-1007
+//     scatter_kernel      slot index to start + cursor (photon_scatter.wgsl:61-71), warp-aggregated
+//     order_kernel        sorts each cell's slot indices ascending: the result is the scatter in slot
+//                         order, independent of atomic arrival order (the reference's order within a
+//                         cell is unspecified)
+//     gather_kernel       sorted[i] = photons[order[i]] (64-byte records)
+#include "rt_kernels.h"
+
+namespace rtd {
+
+namespace {
+
+__device__ __forceinline__ f3 surface_albedo(const DevScene &s, const Mat &m, float u, float v) {
+    if (m.tex_albedo != RT_TEX_NONE) {
+        float4 t = tex_sample(s.tex[RT_TEX_ALBEDO], u, v, (int32_t)m.tex_albedo);
+        return mk3(t.x, t.y, t.z);
+    }
+    return m.albedo;
+}
+
+__device__ __forceinline__ f3 bounce_dir(f3 rd, f3 n, float rough, Rng &rng) {
+    f3 mirror = reflect(rd, n);
+    float blur = smoothstepf(0.0f, 1.0f, rough);
+    if (blur <= 0.001f) return mirror;
+    f3 diff = sample_cosine_hemisphere(rng);
+    return normalize(mix3(mirror, to_world(diff, n), blur));
+}
+
+__device__ __forceinline__ uint32_t cell_key(const rt_grid_params &gp, f3 pos) {
+    uint32_t gx = f2u_sat((pos.x - gp.room_min_x) / gp.cell_size);
+    uint32_t gy = f2u_sat((pos.y - gp.room_min_y) / gp.cell_size);
+    uint32_t gz = f2u_sat((pos.z - gp.room_min_z) / gp.cell_size);
+    return gx + gy * gp.grid_x + gz * gp.grid_x * gp.grid_y;
+}
+
+__device__ __forceinline__ uint32_t slot_key(const rt_grid_params &gp, f3 pos, float power_r) {
+    if (power_r <= 0.0f) return kInvalidKey;
+    uint32_t k = cell_key(gp, pos);
+    return k < gp.num_cells ? k : kInvalidKey;
+}
+
+}  // namespace
+
+constexpr int kTraceBlock = 128;
+
+__global__ void __launch_bounds__(kTraceBlock) photon_trace_kernel(const __grid_constant__ PhotonTraceParams p) {
+    __shared__ uint32_t stack_smem[64 * kTraceBlock];
+    uint32_t *stk = stack_smem + threadIdx.x;
+    const uint32_t stride = kTraceBlock;
+    const uint32_t photon_index = p.photon_begin + blockIdx.x * kTraceBlock + threadIdx.x;
+    if (photon_index >= p.photon_end) return;
+    const DevScene &s = p.scene;
+    const uint32_t num_lights = s.light_count;
+    if (num_lights == 0u) return;
+    Rng rng = rng_init(photon_index * 1103515245u + 12345u);
+    uint32_t li = f2u_sat(rng_f32(rng) * (float)num_lights);
+    li = li < num_lights ? li : num_lights - 1u;
+    const Light light = load_light(s, li);
+    f3 origin = light.data, dir = mk3(0.0f, 0.0f, 1.0f), power = mk3(0.0f, 0.0f, 0.0f);
+    if (light.kind == 0u) {
+        float u1 = 0.0f, u2 = 0.0f;
+        for (uint32_t guard = 0;; ++guard) {
+            u1 = rng_f32(rng) * 2.0f - 1.0f;
+            u2 = rng_f32(rng) * 2.0f - 1.0f;
+            if (u1 * u1 + u2 * u2 < 1.0f) break;
+            if (guard >= (1u << 20)) return;  // bounded; (1 - pi/4)^(2^20) is zero in practice
+        }
+        float z = 1.0f - 2.0f * (u1 * u1 + u2 * u2);
+        float r = sqrtf(1.0f - z * z);
+        dir = normalize(mk3(r * 2.0f * u1, r * 2.0f * u2, z));
+        power = light.color * light.intensity;
+    } else if (light.kind == 1u) {
+        float du = (rng_f32(rng) - 0.5f) * 10.0f;
+        float dv = (rng_f32(rng) - 0.5f) * 10.0f;
+        f3 d = light.data;
+        f3 up = fabsf(d.y) < 0.999f ? mk3(0.0f, 1.0f, 0.0f) : mk3(1.0f, 0.0f, 0.0f);
+        f3 tangent = normalize(cross(up, d));
+        f3 bitangent = cross(d, tangent);
+        origin = du * tangent + dv * bitangent - d * 100.0f;
+        dir = d;
+        power = light.color * light.intensity;
+    } else if (light.kind == 2u) {
+        Tri tri = load_tri_verts(s, f2u_sat(light.data.x));
+        float u1 = rng_f32(rng);
+        float u2 = rng_f32(rng);
+        float su = sqrtf(u1);
+        float u = 1.0f - su;
+        float v = u2 * su;
+        float w = 1.0f - u - v;
+        origin = tri.v0 * u + tri.v1 * v + tri.v2 * w;
+        f3 n = triangle_normal(tri.v0, tri.v1, tri.v2);
+        f3 local = sample_cosine_hemisphere(rng);
+        dir = to_world(local, n);
+        power = light.color * light.intensity;
+    } else if (light.kind == 3u) {
+        const rt_grid_params &gp = p.gp;
+        f3 local = sample_cosine_hemisphere(rng);
+        f3 d = to_world(local, mk3(0.0f, 1.0f, 0.0f));
+        f3 span = mk3((float)gp.grid_x, (float)gp.grid_y, (float)gp.grid_z) * gp.cell_size;
+        f3 center = mk3(gp.room_min_x, gp.room_min_y, gp.room_min_z) + span * 0.5f;
+        float R = fmaxf(fmaxf(span.x, span.y), span.z) * 1.2f + 0.05f;
+        origin = center + d * R;
+        dir = -d;
+        float t = clampf(d.y * 0.5f + 0.5f, 0.0f, 1.0f);
+        power = mix3(light.color, light.data, powf(t, 0.5f)) * light.intensity;
+    } else {
+        return;
+    }
+
+    for (uint32_t bounce = 0; bounce < RT_MAX_BOUNCES; ++bounce) {
+        Hit hit = trace_bvh<64>(s, origin, dir, stk, stride);
+        if (hit.t >= kInf) return;
+        TriFull tri = load_tri(s, hit.prim);
+        Mat mat = load_mat(s, tri.material_id);
+        f3 hit_pos = origin + dir * hit.t;
+        Bary bb = barycentric(tri, origin, dir, hit.t);
+        f3 normal = triangle_normal(tri.v0, tri.v1, tri.v2);
+        bool front = dot(dir, normal) < 0.0f;
+        f3 sn_geom = smooth_normal(tri, bb, normal);
+        f3 face_normal = front ? sn_geom : -sn_geom;
+        f3 shn = face_normal;
+        if (mat.tex_normal != RT_TEX_NONE) {
+            float4 t = tex_sample(s.tex[RT_TEX_NORMAL], bb.uvx, bb.uvy, (int32_t)mat.tex_normal);
+            f3 nm = mk3(t.x, t.y, t.z) * 2.0f - mk3(1.0f, 1.0f, 1.0f);
+            f3 ft, fb;
+            tangent_frame(tri, face_normal, ft, fb);
+            shn = normalize(ft * nm.x + fb * nm.y + face_normal * nm.z);
+        }
+        if ((mat.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && mat.tex_albedo != RT_TEX_NONE) {
+            float alpha = tex_sample(s.tex[RT_TEX_ALBEDO], bb.uvx, bb.uvy, (int32_t)mat.tex_albedo).w;
+            if (alpha < 0.5f) {
+                origin = hit_pos + dir * 0.002f;
+                continue;
+            }
+        }
+        if (mat.tex_emissive != RT_TEX_NONE || len3(mat.emissive) > 1e-4f || mat.kind == 3u) return;
+        if (mat.kind == 2u) {
+            float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
+            float f0s = powf(q, 2.0f);
+            float ct = fabsf(dot(dir, face_normal));
+            float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
+            if (rng_f32(rng) < fr) {
+                dir = reflect(dir, face_normal);
+                origin = hit_pos + face_normal * 0.001f;
+            } else {
+                float eta = front ? 1.0f / mat.ior : mat.ior;
+                dir = refract(dir, face_normal, eta);
+                origin = hit_pos - face_normal * 0.001f;
+            }
+            continue;
+        }
+        const uint64_t slot = (uint64_t)photon_index * 6u + bounce;
+        if (slot < p.slot_count) {
+            float4 *ph = p.photons + 4ull * slot;
+            f3 inc = -dir;
+            ph[0] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.0f);
+            ph[1] = make_float4(power.x, power.y, power.z, 0.0f);
+            ph[2] = make_float4(inc.x, inc.y, inc.z, 0.0f);
+            ph[3] = make_float4(shn.x, shn.y, shn.z, 0.0f);
+            p.keys[slot] = slot_key(p.gp, hit_pos, power.x);
+        }
+        f3 albedo = surface_albedo(s, mat, bb.uvx, bb.uvy);
+        const float mt = mat.metallic;
+        f3 f0 = mk3(0.04f * (1.0f - mt) + albedo.x * mt, 0.04f * (1.0f - mt) + albedo.y * mt,
+                    0.04f * (1.0f - mt) + albedo.z * mt);
+        float ct = fabsf(dot(dir, shn));
+        f3 fr = fresnel_schlick(ct, f0);
+        f3 diffuse_weight = (1.0f - mt) * albedo;
+        float spec_prob = clampf(max3(fr), 0.0f, 0.98f);
+        bool do_spec = rng_f32(rng) < spec_prob;
+        if (do_spec) {
+            dir = bounce_dir(dir, shn, mat.roughness, rng);
+            power = power * f0;
+        } else {
+            f3 local = sample_cosine_hemisphere(rng);
+            dir = to_world(local, shn);
+            power = power * diffuse_weight;
+        }
+        origin = hit_pos + shn * 0.001f;
+        float pr = max3(power);
+        if (pr <= 0.0f || rng_f32(rng) > pr) return;
+        power = power / pr;
+    }
+}
+
+cudaError_t launch_photon_trace(const PhotonTraceParams &p, cudaStream_t st) {
+    if (p.photon_end <= p.photon_begin) return cudaSuccess;
+    uint32_t n = p.photon_end - p.photon_begin;
+    photon_trace_kernel<<<(n + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Keys of a host-provided photon buffer.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) photon_keys_kernel(const float4 *__restrict__ photons, uint64_t n,
+                                                          const rt_grid_params gp, uint32_t *__restrict__ keys) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        float4 a = __ldg(photons + 4 * s), b = __ldg(photons + 4 * s + 1);
+        keys[s] = slot_key(gp, xyz(a), b.x);
+    }
+}
+
+static int g_num_sms = 0;
+static int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        g_num_sms = v > 0 ? v : 1;
+    }
+    return g_num_sms;
+}
+
+cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const rt_grid_params &gp, uint32_t *keys,
+                               cudaStream_t st) {
+    if (slot_count == 0) return cudaSuccess;
+    uint64_t blocks = (slot_count + 255) / 256;
+    uint64_t cap = (uint64_t)num_sms() * 8;
+    photon_keys_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(photons, slot_count, gp, keys);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Grid build
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Histogram.  Lanes of a warp holding the same key are merged (match.any) into one atomic.
+__global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, uint64_t n,
+                                                    uint32_t *__restrict__ counts) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t rounds = (n + stride - 1) / stride;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        uint64_t s = start + r * stride;
+        uint32_t k = s < n ? __ldg(keys + s) : kInvalidKey;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        uint32_t leader = __ffs(peers) - 1;
+        if (k != kInvalidKey && (threadIdx.x & 31u) == leader) atomicAdd(counts + k, (uint32_t)__popc(peers));
+    }
+}
+
+// Slot indices to start[key] + cursor[key]; a warp's lanes with one key take consecutive positions.
+__global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, uint64_t n,
+                                                      const uint2 *__restrict__ meta, uint32_t *__restrict__ cursor,
+                                                      uint32_t *__restrict__ order) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        uint64_t s = start + r * stride;
+        uint32_t k = s < n ? __ldg(keys + s) : kInvalidKey;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        uint32_t leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (k != kInvalidKey && lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        if (k != kInvalidKey) {
+            uint32_t rank = __popc(peers & lanemask_lt());
+            order[__ldg(&meta[k].x) + base + rank] = (uint32_t)s;
+        }
+    }
+}
+
+// Exclusive scan of counts into meta, three phases over tiles of kScanTile cells.
+constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanItems = 8;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+uint32_t grid_scan_partials(uint32_t num_cells) { return (num_cells + kScanTile - 1) / kScanTile + 1; }
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *smem_warp, uint32_t *total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31u) smem_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (kScanThreads / 32) ? smem_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        if (lane < (kScanThreads / 32)) smem_warp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t warp_prefix = warp ? smem_warp[warp - 1] : 0u;
+    if (total) *total = smem_warp[kScanThreads / 32 - 1];
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t *__restrict__ counts, uint32_t n,
+                                                                   uint32_t *__restrict__ partials) {
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanTile;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) {
+        uint32_t c = base + i * kScanThreads + threadIdx.x;
+        if (c < n) sum += __ldg(counts + c);
+    }
+    sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+    if ((threadIdx.x & 31u) == 0) warp_sums[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t w = 0; w < kScanThreads / 32; ++w) t += warp_sums[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
+// One block: exclusive scan of the tile sums in place; partials[ntiles] = grand total.
+__global__ void __launch_bounds__(kScanThreads) scan_partials_kernel(uint32_t *partials, uint32_t ntiles,
+                                                                     uint32_t *total_out) {
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < ntiles; base += kScanThreads) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < ntiles ? partials[i] : 0u;
+        uint32_t tot = 0;
+        uint32_t ex = block_exclusive_scan(v, warp_sums, &tot);
+        if (i < ntiles) partials[i] = carry + ex;
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[ntiles] = carry;
+        if (total_out) *total_out = carry;
+    }
+}
+
+// Rescan each tile with its offset; writes (start, count) per cell.  Items are blocked per thread
+// (thread t owns cells t*8 .. t*8+7 of the tile) so the in-thread sums stay in cell order.
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t *__restrict__ counts, uint32_t n,
+                                                                  const uint32_t *__restrict__ partials,
+                                                                  uint2 *__restrict__ meta) {
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t local = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) {
+        uint32_t c = base + i;
+        v[i] = c < n ? __ldg(counts + c) : 0u;
+        local += v[i];
+    }
+    uint32_t ex = block_exclusive_scan(local, warp_sums, nullptr) + __ldg(partials + blockIdx.x);
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) {
+        uint32_t c = base + i;
+        if (c < n) meta[c] = make_uint2(ex, v[i]);
+        ex += v[i];
+    }
+}
+
+// Ascending sort of one cell's slot indices.  Comparators always order (lower index, higher index)
+// (the "flip" bitonic network), so positions past `count` act as +infinity and are never touched.
+template <typename Seg>
+__device__ __forceinline__ void warp_bitonic(Seg seg, uint32_t count, uint32_t lane) {
+    uint32_t N = 1;
+    while (N < count) N <<= 1;
+    auto cas = [&](uint32_t a, uint32_t b) {
+        if (b < count) {
+            uint32_t x = seg[a], y = seg[b];
+            if (x > y) {
+                seg[a] = y;
+                seg[b] = x;
+            }
+        }
+    };
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        uint32_t hk = k >> 1;
+        for (uint32_t i = lane; i < N / 2; i += 32) {
+            uint32_t a = (i / hk) * k + (i % hk);
+            uint32_t b = a ^ (k - 1);
+            cas(a, b);
+        }
+        __syncwarp();
+        for (uint32_t j = hk >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < N / 2; i += 32) {
+                uint32_t a = (i / j) * (2 * j) + (i % j);
+                cas(a, a + j);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+constexpr uint32_t kOrderWarps = 8;
+constexpr uint32_t kOrderSmem = 1024;  // per-warp shared buffer (entries)
+
+__global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
+                                                                  uint32_t *__restrict__ order) {
+    __shared__ uint32_t buf[kOrderWarps][kOrderSmem];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t warps_total = gridDim.x * kOrderWarps;
+    for (uint32_t c = blockIdx.x * kOrderWarps + w; c < n_cells; c += warps_total) {
+        uint2 m = __ldg(meta + c);
+        const uint32_t start = m.x, count = m.y;
+        if (count <= 1u) continue;
+        if (count <= 32u) {
+            uint32_t v = lane < count ? order[start + lane] : 0xFFFFFFFFu;
+#pragma unroll
+            for (uint32_t k = 2; k <= 32; k <<= 1)
+#pragma unroll
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v, j);
+                    bool up = (lane & k) == 0u;
+                    bool lower = (lane & j) == 0u;
+                    uint32_t mn = min(v, o), mx = max(v, o);
+                    v = (lower == up) ? mn : mx;
+                }
+            if (lane < count) order[start + lane] = v;
+        } else if (count <= kOrderSmem) {
+            uint32_t *sb = buf[w];
+            for (uint32_t i = lane; i < count; i += 32) sb[i] = order[start + i];
+            __syncwarp();
+            warp_bitonic(sb, count, lane);
+            for (uint32_t i = lane; i < count; i += 32) order[start + i] = sb[i];
+            __syncwarp();
+        } else {
+            warp_bitonic(order + start, count, lane);
+        }
+    }
+}
+
+// sorted[i] = photons[order[i]] for i < total.
+__global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__restrict__ photons,
+                                                            const uint32_t *__restrict__ order,
+                                                            const uint32_t *__restrict__ total, uint64_t cap,
+                                                            float4 *__restrict__ sorted) {
+    const uint64_t n = min((uint64_t)__ldg(total), cap);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 *src = photons + 4ull * __ldg(order + i);
+        float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
+        float4 *dst = sorted + 4ull * i;
+        dst[0] = a;
+        dst[1] = b;
+        dst[2] = c;
+        dst[3] = d;
+    }
+}
+
+cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
+    cudaError_t e;
+    const uint32_t C = g.num_cells;
+    if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(g.cursor, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+    const uint64_t n = g.slot_count;
+    const uint32_t sm = (uint32_t)num_sms();
+    auto grid_for = [&](uint64_t items, uint32_t block, uint32_t per_sm) {
+        uint64_t b = (items + block - 1) / block;
+        uint64_t cap = (uint64_t)sm * per_sm;
+        return (unsigned)(b < 1 ? 1 : (b < cap ? b : cap));
+    };
+    if (n) {
+        count_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
+    scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
+    scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
+    scan_apply_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (n) {
+        scatter_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
+        order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(g.meta, C, g.order);
+        photon_gather_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace rtd

@@ -1,0 +1,346 @@
+// Device-side building blocks of the sm_103a hot path: vector math, the PCG hash RNG, rgba8 texture
+// sampling, Moller-Trumbore, BVH traversal, hit shading and the BSDF pieces.
+//
+// Numerics follow the WGSL sources term by term (rustracer-renderer/shaders/common.wgsl, gather.wgsl,
+// photon_trace.wgsl); the library is compiled with --fmad=false and IEEE division / square root so
+// a product a*b+c is rounded twice, as the shaders' separate multiply and add are.  WGSL leaves a
+// few behaviours to the backend; this implementation fixes them as:
+//   * min/max with one NaN operand return the other (fminf/fmaxf);
+//   * float -> u32/i32 conversion truncates toward zero and saturates, NaN -> 0;
+//   * an out-of-range buffer index is clamped to the last element;
+//   * normalize(v) = v * (1/sqrt(dot(v,v))), inverseSqrt(x) = 1/sqrt(x), mix(a,b,t) = a(1-t) + bt;
+//   * textureSampleLevel(level 0, linear, repeat, rgba8unorm) = fp32 bilinear of byte/255 texels with
+//     the array layer clamped to the layer count (an empty role samples as zero).
+#pragma once
+#include <cstdint>
+
+#include "../../include/rustracer_cuda.h"
+
+namespace rtd {
+
+constexpr float kPi = 3.141592653589793f;
+constexpr float kInf = 1e38f;
+constexpr float kEps = 1e-6f;
+constexpr uint32_t kInvalidKey = 0xFFFFFFFFu;
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 xyz(float4 a) { return f3{a.x, a.y, a.z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator/(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float len3(f3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
+__device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
+__device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float max3(f3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
+__device__ __forceinline__ f3 mix3(f3 a, f3 b, float t) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
+    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+__device__ __forceinline__ uint32_t f2u_sat(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return __float2uint_rz(f);
+}
+__device__ __forceinline__ int32_t f2i_sat(float f) {
+    if (f != f) return 0;
+    if (f <= -2147483648.0f) return INT32_MIN;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    return __float2int_rz(f);
+}
+
+__device__ __forceinline__ f3 reflect(f3 v, f3 n) { return v - 2.0f * dot(v, n) * n; }
+__device__ __forceinline__ f3 refract(f3 v, f3 n, float eta) {
+    float cos_theta = fminf(dot(-v, n), 1.0f);
+    f3 perp = eta * (v + cos_theta * n);
+    f3 par = -sqrtf(fabsf(1.0f - dot(perp, perp))) * n;
+    return perp + par;
+}
+__device__ __forceinline__ f3 fresnel_schlick(float cos_theta, f3 f0) {
+    float p = powf(clampf(1.0f - cos_theta, 0.0f, 1.0f), 5.0f);
+    return f0 + (mk3(1.0f, 1.0f, 1.0f) - f0) * p;
+}
+
+// ---- PCG hash RNG (common.wgsl:29-52) ----------------------------------------------------------
+struct Rng {
+    uint32_t state;  // inc is always 1 in the reference
+};
+__device__ __forceinline__ Rng rng_init(uint32_t seed) {
+    uint32_t s = seed * 747796405u + 2891336453u;
+    s = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    return Rng{s};
+}
+__device__ __forceinline__ uint32_t rng_next(Rng &r) {
+    uint32_t old = r.state;
+    r.state = old * 747796405u + 1u;
+    uint32_t word = ((old >> ((old >> 28u) + 4u)) ^ old) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+// f32(u32) rounds to nearest even; the division by 2^32 is exact.
+__device__ __forceinline__ float rng_f32(Rng &r) { return __uint2float_rn(rng_next(r)) * 2.3283064365386963e-10f; }
+
+__device__ __forceinline__ f3 sample_cosine_hemisphere(Rng &r) {
+    float u1 = rng_f32(r);
+    float u2 = rng_f32(r);
+    float phi = 2.0f * kPi * u1;
+    float ct = sqrtf(u2);
+    float st = sqrtf(1.0f - u2);
+    return mk3(cosf(phi) * st, ct, sinf(phi) * st);
+}
+__device__ __forceinline__ f3 to_world(f3 local, f3 n) {
+    f3 up = fabsf(n.y) < 0.999f ? mk3(0.0f, 1.0f, 0.0f) : mk3(1.0f, 0.0f, 0.0f);
+    f3 t = normalize(cross(up, n));
+    f3 b = cross(n, t);
+    return t * local.x + n * local.y + b * local.z;
+}
+
+// ---- scene views ------------------------------------------------------------------------------
+struct DevTex {
+    const uchar4 *texels;  // layer-major, row-major
+    uint32_t width, height, layers;
+};
+
+struct DevScene {
+    const float4 *nodes;     // 3 x float4 per BVHNode
+    const uint32_t *prims;
+    const float4 *tris;      // 8 x float4 per TriangleGpu
+    const float4 *mats;      // 4 x float4 per MaterialGpu
+    const float4 *lights;    // 4 x float4 per LightGpu
+    uint32_t node_count, prim_count, tri_count, mat_count, light_count;
+    DevTex tex[4];
+    // The first environment light (gather.wgsl:276-289), resolved on the host.
+    float env_intensity;
+    float env_color[3];
+    float env_horizon[3];
+};
+
+__device__ __forceinline__ uint32_t clampi_u(uint32_t i, uint32_t n) { return i < n ? i : n - 1u; }
+
+struct Tri {
+    f3 v0, v1, v2;
+};
+__device__ __forceinline__ Tri load_tri_verts(const DevScene &s, uint32_t i) {
+    const float4 *p = s.tris + 8ull * clampi_u(i, s.tri_count);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    return Tri{xyz(a), xyz(b), xyz(c)};
+}
+struct TriFull {
+    f3 v0, v1, v2, n0, n1, n2;
+    float uv0x, uv0y, uv1x, uv1y, uv2x, uv2y;
+    uint32_t material_id;
+};
+__device__ __forceinline__ TriFull load_tri(const DevScene &s, uint32_t i) {
+    const float4 *p = s.tris + 8ull * clampi_u(i, s.tri_count);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3), e = __ldg(p + 4), f = __ldg(p + 5),
+           g = __ldg(p + 6), h = __ldg(p + 7);
+    TriFull t;
+    t.v0 = xyz(a); t.v1 = xyz(b); t.v2 = xyz(c);
+    t.n0 = xyz(d); t.n1 = xyz(e); t.n2 = xyz(f);
+    t.uv0x = g.x; t.uv0y = g.y; t.uv1x = g.z; t.uv1y = g.w; t.uv2x = h.x; t.uv2y = h.y;
+    t.material_id = __float_as_uint(h.z);
+    return t;
+}
+struct Mat {
+    f3 albedo;
+    float alpha;
+    f3 emissive;
+    float roughness, metallic, ior;
+    uint32_t kind, flags, tex_albedo, tex_mr, tex_emissive, tex_normal;
+};
+__device__ __forceinline__ Mat load_mat(const DevScene &s, uint32_t i) {
+    const float4 *p = s.mats + 4ull * clampi_u(i, s.mat_count);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+    Mat m;
+    m.albedo = xyz(a);
+    m.alpha = a.w;
+    m.emissive = xyz(b);
+    m.roughness = b.w;
+    m.metallic = c.x;
+    m.ior = c.y;
+    m.kind = __float_as_uint(c.z);
+    m.flags = __float_as_uint(c.w);
+    m.tex_albedo = __float_as_uint(d.x);
+    m.tex_mr = __float_as_uint(d.y);
+    m.tex_emissive = __float_as_uint(d.z);
+    m.tex_normal = __float_as_uint(d.w);
+    return m;
+}
+struct Light {
+    f3 data;
+    float data_w;
+    f3 color;
+    float intensity;
+    uint32_t kind;
+};
+__device__ __forceinline__ Light load_light(const DevScene &s, uint32_t i) {
+    const float4 *p = s.lights + 4ull * i;
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    return Light{xyz(a), a.w, xyz(b), b.w, __float_as_uint(c.x)};
+}
+
+// textureSampleLevel on an rgba8unorm array with a linear / repeat sampler, level 0.
+__device__ __forceinline__ float4 tex_sample(const DevTex &t, float u, float v, int32_t layer) {
+    if (t.texels == nullptr) return make_float4(0.f, 0.f, 0.f, 0.f);
+    int32_t L = layer < 0 ? 0 : (layer >= (int32_t)t.layers ? (int32_t)t.layers - 1 : layer);
+    const uint32_t W = t.width, H = t.height;
+    float fu = u - floorf(u), fv = v - floorf(v);
+    if (!(fu >= 0.0f)) fu = 0.0f;
+    if (!(fv >= 0.0f)) fv = 0.0f;
+    float x = fu * (float)W - 0.5f, y = fv * (float)H - 0.5f;
+    float x0f = floorf(x), y0f = floorf(y);
+    float ax = x - x0f, ay = y - y0f;
+    int32_t x0 = (int32_t)x0f, y0 = (int32_t)y0f;
+    if (x0 < 0) x0 += (int32_t)W;
+    if (y0 < 0) y0 += (int32_t)H;
+    if (x0 >= (int32_t)W) x0 -= (int32_t)W;
+    if (y0 >= (int32_t)H) y0 -= (int32_t)H;
+    int32_t x1 = x0 + 1 == (int32_t)W ? 0 : x0 + 1;
+    int32_t y1 = y0 + 1 == (int32_t)H ? 0 : y0 + 1;
+    const uchar4 *base = t.texels + (size_t)L * W * H;
+    uchar4 t00 = __ldg(base + (size_t)y0 * W + x0), t10 = __ldg(base + (size_t)y0 * W + x1);
+    uchar4 t01 = __ldg(base + (size_t)y1 * W + x0), t11 = __ldg(base + (size_t)y1 * W + x1);
+    auto lerp2 = [&](unsigned char a, unsigned char b, unsigned char c, unsigned char d) {
+        float fa = (float)a / 255.0f, fb = (float)b / 255.0f, fc = (float)c / 255.0f, fd = (float)d / 255.0f;
+        float top = fa * (1.0f - ax) + fb * ax;
+        float bot = fc * (1.0f - ax) + fd * ax;
+        return top * (1.0f - ay) + bot * ay;
+    };
+    return make_float4(lerp2(t00.x, t10.x, t01.x, t11.x), lerp2(t00.y, t10.y, t01.y, t11.y),
+                       lerp2(t00.z, t10.z, t01.z, t11.z), lerp2(t00.w, t10.w, t01.w, t11.w));
+}
+
+// ---- Moller-Trumbore (common.wgsl:78-100) ------------------------------------------------------
+__device__ __forceinline__ float intersect_triangle(f3 ro, f3 rd, f3 v0, f3 v1, f3 v2) {
+    f3 e1 = v1 - v0;
+    f3 e2 = v2 - v0;
+    f3 h = cross(rd, e2);
+    float a = dot(e1, h);
+    if (fabsf(a) < 1e-7f) return kInf;
+    float f = 1.0f / a;
+    f3 s = ro - v0;
+    float u = f * dot(s, h);
+    if (u < 0.0f || u > 1.0f) return kInf;
+    f3 q = cross(s, e1);
+    float v = f * dot(rd, q);
+    if (v < 0.0f || u + v > 1.0f) return kInf;
+    float t = f * dot(e2, q);
+    if (t > kEps) return t;
+    return kInf;
+}
+
+struct Hit {
+    float t;
+    uint32_t prim;
+};
+
+// Closest hit by the reference's traversal (gather.wgsl:66-88): 64-entry stack, left child first,
+// right child pushed (dropped when 63 entries are in use), every primitive of a visited leaf tested,
+// first strictly-smaller t wins.  The stack lives in shared memory, one column per thread.
+template <int kStack>
+__device__ __forceinline__ Hit trace_bvh(const DevScene &s, f3 ro, f3 rd, uint32_t *stk, uint32_t stride) {
+    Hit hit{kInf, 0u};
+    if (s.node_count == 0u) return hit;
+    f3 inv = mk3(1.0f, 1.0f, 1.0f) / rd;
+    uint32_t idx = 0u, sp = 0u;
+    for (;;) {
+        const float4 *np = s.nodes + 3ull * clampi_u(idx, s.node_count);
+        float4 a = __ldg(np), b = __ldg(np + 1);
+        uint32_t pc = __ldg(reinterpret_cast<const uint32_t *>(np + 2));
+        f3 t0 = (xyz(a) - ro) * inv;
+        f3 t1 = (xyz(b) - ro) * inv;
+        f3 tm = vmin(t0, t1);
+        f3 tx = vmax(t0, t1);
+        float te = fmaxf(fmaxf(tm.x, tm.y), tm.z);
+        float ta = fminf(fminf(tx.x, tx.y), tx.z);
+        if (te <= ta && ta > 0.0f && te < hit.t) {
+            uint32_t lf = __float_as_uint(a.w);
+            if (pc > 0u) {
+                for (uint32_t i = 0; i < pc; ++i) {
+                    uint32_t slot = clampi_u(lf + i, s.prim_count);
+                    uint32_t pi = __ldg(s.prims + slot);
+                    Tri tr = load_tri_verts(s, pi);
+                    float t = intersect_triangle(ro, rd, tr.v0, tr.v1, tr.v2);
+                    if (t < hit.t) {
+                        hit.t = t;
+                        hit.prim = pi;
+                    }
+                }
+                if (sp == 0u) break;
+                sp -= 1u;
+                idx = stk[sp * stride];
+            } else {
+                if (sp < (uint32_t)(kStack - 1)) {
+                    stk[sp * stride] = __float_as_uint(b.w);
+                    sp += 1u;
+                }
+                idx = lf;
+            }
+        } else {
+            if (sp == 0u) break;
+            sp -= 1u;
+            idx = stk[sp * stride];
+        }
+    }
+    return hit;
+}
+
+struct Bary {
+    float uvx, uvy, u, v;
+};
+__device__ __forceinline__ Bary barycentric(const TriFull &tri, f3 ro, f3 rd, float t) {
+    f3 e1 = tri.v1 - tri.v0;
+    f3 e2 = tri.v2 - tri.v0;
+    f3 p = ro + rd * t - tri.v0;
+    float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2);
+    float d20 = dot(p, e1), d21 = dot(p, e2);
+    float denom = d00 * d11 - d01 * d01;
+    float u = 0.0f, v = 0.0f;
+    if (denom != 0.0f) {
+        u = (d11 * d20 - d01 * d21) / denom;
+        v = (d00 * d21 - d01 * d20) / denom;
+    }
+    float w = 1.0f - u - v;
+    return Bary{tri.uv0x * w + tri.uv1x * u + tri.uv2x * v, tri.uv0y * w + tri.uv1y * u + tri.uv2y * v, u, v};
+}
+__device__ __forceinline__ f3 smooth_normal(const TriFull &tri, const Bary &b, f3 geometric) {
+    float w = 1.0f - b.u - b.v;
+    f3 n = tri.n0 * w + tri.n1 * b.u + tri.n2 * b.v;
+    if (dot(n, n) < 1e-8f) return geometric;
+    return normalize(n);
+}
+__device__ __forceinline__ void tangent_frame(const TriFull &tri, f3 n, f3 &t_out, f3 &b_out) {
+    f3 e1 = tri.v1 - tri.v0;
+    f3 e2 = tri.v2 - tri.v0;
+    float d1x = tri.uv1x - tri.uv0x, d1y = tri.uv1y - tri.uv0y;
+    float d2x = tri.uv2x - tri.uv0x, d2y = tri.uv2y - tri.uv0y;
+    float det = d1x * d2y - d2x * d1y;
+    float f = fabsf(det) < 1e-12f ? 0.0f : 1.0f / det;
+    f3 t = (e1 * d2y - e2 * d1y) * f;
+    f3 b = (e2 * d1x - e1 * d2x) * f;
+    f3 tt = t - n * dot(n, t);
+    if (dot(tt, tt) < 1e-10f) {
+        tt = cross(n, mk3(1.0f, 0.0f, 0.0f));
+        if (dot(tt, tt) < 1e-6f) tt = cross(n, mk3(0.0f, 1.0f, 0.0f));
+    }
+    tt = normalize(tt);
+    f3 c = cross(n, tt);
+    t_out = tt;
+    b_out = c * (dot(c, b) > 0.0f ? 1.0f : -1.0f);
+}
+__device__ __forceinline__ f3 triangle_normal(f3 v0, f3 v1, f3 v2) { return normalize(cross(v1 - v0, v2 - v0)); }
+
+}  // namespace rtd

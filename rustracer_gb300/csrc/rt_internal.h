@@ -1,0 +1,76 @@
+// Internal host-side helpers shared by the translation units of librustracer_cuda.
+#pragma once
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/rustracer_cuda.h"
+#include "rt_layout_check.h"
+
+namespace rt {
+
+// Thread-local error message returned by rt_last_error().
+void set_error(const char *fmt, ...)
+#if defined(__GNUC__)
+    __attribute__((format(printf, 1, 2)))
+#endif
+    ;
+void clear_error();
+
+struct Vec3 {
+    float x, y, z;
+};
+inline Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
+inline Vec3 operator+(Vec3 a, Vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline Vec3 operator-(Vec3 a, Vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline Vec3 operator*(Vec3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline Vec3 operator/(Vec3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+inline float dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline Vec3 cross(Vec3 a, Vec3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+Vec3 normalize(Vec3 a);  // a * (1 / |a|), glam's Vec3::normalize
+
+struct Mesh {
+    std::vector<Vec3> positions, normals;
+    std::vector<float> uvs;  // 2 per vertex
+    std::vector<uint32_t> indices;
+    uint32_t material_id = 0;
+    // Optional per-triangle material ids (overrides material_id when non-empty).
+    std::vector<uint32_t> tri_materials;
+};
+
+struct Texture {
+    uint32_t width = 0, height = 0, layers = 0;
+    std::vector<uint8_t> rgba8;
+};
+
+struct BVH {
+    std::vector<rt_bvh_node> nodes;
+    std::vector<uint32_t> prims;
+};
+
+// BVHBuilder::build (rustracer-core/src/bvh.rs:135-336).
+BVH build_bvh(const std::vector<Vec3> &centroids, const std::vector<Vec3> &bmin, const std::vector<Vec3> &bmax);
+
+}  // namespace rt
+
+struct rt_scene {
+    std::vector<rt::Mesh> meshes;
+    std::vector<rt_material> materials;
+    std::vector<rt_light> lights;
+    rt::Texture tex[4];
+    // Flattened state (rt_scene_finalize).
+    bool finalized = false;
+    std::vector<rt_triangle> triangles;
+    rt::BVH bvh;
+    float bounds_min[3] = {0, 0, 0}, bounds_max[3] = {0, 0, 0};
+    bool has_bounds = false;
+    // Preferred camera of a procedural scene (rt_scene_default_camera).
+    bool has_camera = false;
+    rt_camera camera{};
+};
+
+struct rt_bvh {
+    rt::BVH b;
+};

@@ -1,0 +1,68 @@
+// Kernel parameter blocks and host-side launchers of the hot-path kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rt_device.cuh"
+
+namespace rtd {
+
+struct GatherParams {
+    DevScene scene;
+    rt_camera_uniform cam;
+    rt_image_params ip;
+    rt_grid_params gp;
+    const float4 *sorted_photons;  // 4 x float4 per photon
+    uint64_t sorted_count;
+    const uint2 *grid_meta;        // (start, count) per cell
+    uint32_t max_bounces;
+    float4 *frame;
+    float4 *moments;
+    float4 *gbuffer;
+    unsigned long long *counters;  // [0] segments, [1] shadow rays
+};
+__global__ void gather_kernel(const __grid_constant__ GatherParams p);
+
+struct PhotonTraceParams {
+    DevScene scene;
+    rt_grid_params gp;
+    uint32_t photon_begin, photon_end;  // photon indices traced by this launch
+    uint64_t slot_count;                // photon_slots
+    float4 *photons;                    // 4 x float4 per slot
+    uint32_t *keys;                     // cell key per slot (kInvalidKey when not binned)
+};
+__global__ void photon_trace_kernel(const __grid_constant__ PhotonTraceParams p);
+
+// Launchers (stream-ordered, no synchronisation).  Each returns the launch error, if any.
+cudaError_t launch_gather(const GatherParams &p, cudaStream_t st);
+cudaError_t launch_photon_trace(const PhotonTraceParams &p, cudaStream_t st);
+
+// Photon grid (exact u32 counting sort).  Scratch sizes come from grid_scratch_bytes.
+struct GridBuffers {
+    const float4 *photons;  // slot_count photons
+    const uint32_t *keys;   // slot_count keys
+    uint64_t slot_count;
+    uint32_t num_cells;
+    uint32_t *counts;       // num_cells
+    uint2 *meta;            // num_cells
+    uint32_t *cursor;       // num_cells
+    uint32_t *order;        // slot_count: slot indices in (cell, slot) order
+    float4 *sorted;         // slot_count photons
+    uint32_t *scan_partials;  // grid_scan_partials(num_cells) entries
+    uint32_t *total;          // 1 entry: number of binned photons
+};
+uint32_t grid_scan_partials(uint32_t num_cells);
+cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const rt_grid_params &gp, uint32_t *keys,
+                               cudaStream_t st);
+// count -> scan -> scatter -> per-cell slot order -> photon gather.  counts/cursor are cleared here.
+cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st);
+
+// Image kernels.
+cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
+                           const rt_denoise_params &p, cudaStream_t st);
+// accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass.
+cudaError_t launch_resolve(const float4 *frame, float4 *accum, const float4 *gbuffer, uint32_t width,
+                           uint32_t height, float alpha, const rt_tonemap_params &tp, uchar4 *out, cudaStream_t st);
+
+}  // namespace rtd
