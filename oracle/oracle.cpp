@@ -245,15 +245,19 @@ struct Hit {
     uint32_t prim_id;
 };
 
+// An empty array reads as one zero element (the index clamp then has a target).
+static const rt_triangle kZeroTri = {};
+static const rt_material kZeroMat = {};
+
 struct Scene {
     const rt_scene_desc *d;
     const rt_triangle &tri(uint32_t i) const {
         uint64_t n = d->triangle_count;
-        return d->triangles[i < n ? i : n - 1];
+        return n ? d->triangles[i < n ? i : n - 1] : kZeroTri;
     }
     const rt_material &mat(uint32_t i) const {
         uint64_t n = d->material_count;
-        return d->materials[i < n ? i : n - 1];
+        return n ? d->materials[i < n ? i : n - 1] : kZeroMat;
     }
     // gather.wgsl:66-88 (photon_trace.wgsl:31-81 is the same traversal)
     // nodes / tris (optional): node fetches and triangle tests, the traversal's algorithmic work.
@@ -278,7 +282,9 @@ struct Scene {
                 if (n.prim_count > 0u) {
                     for (uint32_t i = 0; i < n.prim_count; ++i) {
                         uint64_t slot = (uint64_t)n.left_first + i;
-                        uint32_t pi = d->bvh_prims[slot < d->bvh_prim_count ? slot : d->bvh_prim_count - 1];
+                        uint32_t pi = d->bvh_prim_count
+                                          ? d->bvh_prims[slot < d->bvh_prim_count ? slot : d->bvh_prim_count - 1]
+                                          : 0u;
                         const rt_triangle &tr = tri(pi);
                         ++n_tris;
                         float t = intersect_triangle(ro, rd, ld(tr.v0), ld(tr.v1), ld(tr.v2));

@@ -128,7 +128,8 @@ struct DevScene {
     float env_horizon[3];
 };
 
-__device__ __forceinline__ uint32_t clampi_u(uint32_t i, uint32_t n) { return i < n ? i : n - 1u; }
+// Index clamped into [0, n) (n == 0 maps to element 0, which every scene array has).
+__device__ __forceinline__ uint32_t clampi_u(uint32_t i, uint32_t n) { return i < n ? i : (n ? n - 1u : 0u); }
 
 struct Tri {
     f3 v0, v1, v2;

@@ -149,10 +149,13 @@ void resolve_env(rt_renderer *r) {
         }
 }
 
+// Every scene array gets at least one (zeroed) element, so a clamped index is always in bounds.
 template <class T>
 int upload(DevBuf &b, const T *src, uint64_t n, cudaStream_t st) {
-    RT_CK(b.alloc(sizeof(T) * n));
+    const size_t bytes = sizeof(T) * (n ? n : 1);
+    RT_CK(b.alloc(bytes));
     if (n) RT_CK(cudaMemcpyAsync(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    else RT_CK(cudaMemsetAsync(b.p, 0, bytes, st));
     return RT_OK;
 }
 
