@@ -123,6 +123,7 @@ class Scene:
             handle = h.value
         self._h = C.c_void_p(handle)
         self._desc: A.SceneDesc | None = None
+        self._n_materials = None
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -159,9 +160,13 @@ class Scene:
         self._desc = None
 
     def add_material(self, m: A.Material) -> int:
+        """Appends a material; returns its index."""
+        if self._n_materials is None:
+            self._n_materials = self.describe().material_count
         A.check("rt_scene_add_material", A.load().rt_scene_add_material(self._h, C.byref(m)))
         self._desc = None
-        return self.describe().material_count - 1
+        self._n_materials += 1
+        return self._n_materials - 1
 
     def add_light(self, l: A.Light) -> None:
         A.check("rt_scene_add_light", A.load().rt_scene_add_light(self._h, C.byref(l)))
@@ -199,13 +204,14 @@ class Scene:
 
     # ---- numpy views of the flattened arrays -----------------------------------------------------
     def arrays(self) -> dict[str, np.ndarray]:
+        """Copies of the flattened arrays (safe to keep after the scene is gone)."""
         d = self.describe()
 
         def view(p, n, struct):
             if n == 0:
                 return np.zeros(0, dtype=A.np_dtype(struct))
             return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint8)), shape=(n * C.sizeof(struct),)).view(
-                A.np_dtype(struct))
+                A.np_dtype(struct)).copy()
 
         out = {
             "triangles": view(d.triangles, d.triangle_count, A.Triangle),
@@ -213,7 +219,7 @@ class Scene:
             "materials": view(d.materials, d.material_count, A.Material),
             "lights": view(d.lights, d.light_count, A.Light),
         }
-        out["bvh_prims"] = (np.ctypeslib.as_array(d.bvh_prims, shape=(d.bvh_prim_count,))
+        out["bvh_prims"] = (np.ctypeslib.as_array(d.bvh_prims, shape=(d.bvh_prim_count,)).copy()
                             if d.bvh_prim_count else np.zeros(0, np.uint32))
         return out
 
