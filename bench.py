@@ -41,6 +41,9 @@ import numpy as np  # noqa: E402
 WORKLOADS = {
     "icosphere1080p": dict(scene="icosphere", level=8, seed=0, sigma=0.02, tex=1024, width=1920, height=1080, spp=4,
                            max_bounces=8, accumulate_frames=32, denoise=False, photons=0),
+    # the same scene at 480x270 (for profiler captures of one gather launch)
+    "icosphere270p": dict(scene="icosphere", level=8, seed=0, sigma=0.02, tex=1024, width=480, height=270, spp=4,
+                          max_bounces=8, accumulate_frames=32, denoise=False, photons=0),
     "cornell256": dict(scene="cornell", width=256, height=256, spp=1, max_bounces=6, accumulate_frames=16,
                        denoise=False, photons=0),
 }
