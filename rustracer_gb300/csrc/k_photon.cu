@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kTraceBlock) photon_trace_kernel(const __grid_
     }
 
     for (uint32_t bounce = 0; bounce < RT_MAX_BOUNCES; ++bounce) {
-        Hit hit = trace_bvh<64>(s, origin, dir, stk, stride);
+        Hit hit = trace<false>(s, origin, dir, kInf, stk, stride);
         if (hit.t >= kInf) return;
         TriFull tri = load_tri(s, hit.prim);
         Mat mat = load_mat(s, tri.material_id);
@@ -209,16 +209,13 @@ __global__ void __launch_bounds__(256) photon_keys_kernel(const float4 *__restri
     }
 }
 
-static int g_num_sms = 0;
-static int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        g_num_sms = v > 0 ? v : 1;
-    }
-    return g_num_sms;
+int device_sm_count() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
 }
+static int num_sms() { return device_sm_count(); }
 
 cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const rt_grid_params &gp, uint32_t *keys,
                                cudaStream_t st) {

@@ -1,0 +1,684 @@
+// The gather pass as a wavefront: rustracer-renderer/shaders/gather.wgsl:258-594 split into kernels that
+// each run one uniform piece of code over a compacted queue of paths.
+//
+//   generate   camera ray of sample 0 for every pixel (gather.wgsl:262-297); fills queue 0
+//   extend     closest hit of every queued path (gather.wgsl:300)
+//   shade      one loop body of gather.wgsl:299-537 per queued path: hit shading, emission, debug
+//              views, dielectric / metallic-roughness lobes, the light sample of NEE
+//              (gather.wgsl:152-206, its shadow ray deferred to `shadow`), photon lookup, next
+//              direction, Russian roulette; a finished sample starts the pixel's next sample in the
+//              same slot; continuing paths are appended to the next queue (warp ballot + one atomic)
+//   shadow     occlusion of each deferred NEE ray; a visible light adds its contribution
+//   finalize   sigma clamp and the frame / moments / gbuffer writes (gather.wgsl:548-593)
+//
+// One path slot per pixel: a pixel's samples run one after the other in its slot, with one RNG
+// stream, exactly as the reference's per-pixel loop.  Every pixel receives its contributions in the
+// reference's order except that a bounce's NEE term lands after that bounce's other terms; floating
+// point addition order is the only difference (an ulp).  The host launches spp * max_bounces
+// iterations; a path extends at most once per iteration, so that bounds every pixel's segments.
+#include "rt_kernels.h"
+
+namespace rtd {
+
+namespace {
+
+__device__ __forceinline__ float luma(f3 c) { return dot(c, mk3(0.2126f, 0.7152f, 0.0722f)); }
+
+struct Accum {
+    f3 col;
+    float lum_sum, lum2_sum;
+    float sl[8];
+};
+__device__ __forceinline__ void add_radiance(uint32_t s, Accum &a, f3 c) {
+    a.col = a.col + c;
+    float l = luma(c);
+    a.lum_sum += l;
+    a.lum2_sum += l * l;
+    if (s < 8u) a.sl[s] += l;
+}
+__device__ __forceinline__ void add_luma(uint32_t s, Accum &a, f3 c) {
+    float l = luma(c);
+    a.lum_sum += l;
+    a.lum2_sum += l * l;
+    if (s < 8u) a.sl[s] += l;
+}
+__device__ __forceinline__ Accum load_acc(const WaveParams &p, uint32_t pix) {
+    const float4 a = p.acc[4 * (size_t)pix], b = p.acc[4 * (size_t)pix + 1], c = p.acc[4 * (size_t)pix + 2],
+                 d = p.acc[4 * (size_t)pix + 3];
+    Accum A;
+    A.col = mk3(a.x, a.y, a.z);
+    A.lum_sum = a.w;
+    A.lum2_sum = b.x;
+    A.sl[0] = c.x; A.sl[1] = c.y; A.sl[2] = c.z; A.sl[3] = c.w;
+    A.sl[4] = d.x; A.sl[5] = d.y; A.sl[6] = d.z; A.sl[7] = d.w;
+    return A;
+}
+__device__ __forceinline__ void store_acc(const WaveParams &p, uint32_t pix, const Accum &A, float4 b_rest) {
+    p.acc[4 * (size_t)pix] = make_float4(A.col.x, A.col.y, A.col.z, A.lum_sum);
+    p.acc[4 * (size_t)pix + 1] = make_float4(A.lum2_sum, b_rest.y, b_rest.z, b_rest.w);
+    p.acc[4 * (size_t)pix + 2] = make_float4(A.sl[0], A.sl[1], A.sl[2], A.sl[3]);
+    p.acc[4 * (size_t)pix + 3] = make_float4(A.sl[4], A.sl[5], A.sl[6], A.sl[7]);
+}
+
+__device__ __forceinline__ f3 sky_color(f3 dir, f3 zenith, f3 horizon, float intensity) {
+    float t = clampf(dir.y * 0.5f + 0.5f, 0.0f, 1.0f);
+    return mix3(horizon, zenith, powf(t, 0.5f)) * intensity;
+}
+__device__ __forceinline__ float smith_g1(float nd, float a) {
+    float k = a * 0.5f;
+    return nd / (nd * (1.0f - k) + k);
+}
+__device__ __forceinline__ f3 spec_ggx(f3 wo, f3 n, f3 wi, float a, f3 f0) {
+    float ndl = dot(n, wi);
+    float ndv = dot(n, wo);
+    if (ndl <= 0.0f || ndv <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+    f3 h = normalize(wo + wi);
+    float ndh = fmaxf(dot(n, h), 0.0f);
+    float a2 = a * a;
+    float dd = ndh * ndh * (a2 - 1.0f) + 1.0f;
+    float D = a2 / (kPi * dd * dd);
+    f3 F = fresnel_schlick(fmaxf(dot(wo, h), 0.0f), f0);
+    return F * (D * smith_g1(ndl, a) * smith_g1(ndv, a) / (4.0f * ndl * ndv));
+}
+__device__ __forceinline__ f3 sample_spec_dir(f3 rd, f3 n, float a, Rng &rng) {
+    f3 up = fabsf(n.y) < 0.999f ? mk3(0.0f, 1.0f, 0.0f) : mk3(1.0f, 0.0f, 0.0f);
+    f3 bt = normalize(cross(up, n));
+    f3 bb = cross(n, bt);
+    f3 mrd = -rd;
+    f3 v = mk3(dot(bt, mrd), dot(bb, mrd), dot(n, mrd));
+    f3 vh = normalize(mk3(a * v.x, a * v.y, fmaxf(v.z, 1e-4f)));
+    float l2 = vh.x * vh.x + vh.y * vh.y;
+    f3 t1 = l2 > 0.0f ? mk3(-vh.y, vh.x, 0.0f) * (1.0f / sqrtf(l2)) : mk3(1.0f, 0.0f, 0.0f);
+    f3 t2 = cross(vh, t1);
+    float r = sqrtf(rng_f32(rng));
+    float phi = 2.0f * kPi * rng_f32(rng);
+    float x = r * cosf(phi);
+    float y = r * sinf(phi);
+    float s = 0.5f * (1.0f + vh.z);
+    float yy = (1.0f - s) * sqrtf(fmaxf(0.0f, 1.0f - x * x)) + s * y;
+    f3 hh = x * t1 + yy * t2 + sqrtf(fmaxf(0.0f, 1.0f - x * x - yy * yy)) * vh;
+    f3 hn = normalize(hh);
+    f3 m = bt * hn.x + bb * hn.y + n * hn.z;
+    f3 out = reflect(rd, m);
+    return dot(out, n) > 0.0f ? out : reflect(rd, n);
+}
+
+// The light sample of direct_light (gather.wgsl:152-206) up to its shadow query.  `occlude` is set
+// when the sample needs the shadow ray (origin o, direction ld, max_dist); e is the unoccluded value.
+struct LightSample {
+    f3 e, wi, o;
+    float max_dist;
+    bool occlude;
+};
+__device__ __forceinline__ LightSample light_sample(const WaveParams &p, f3 hp, f3 sn, Rng &rng) {
+    const DevScene &s = p.scene;
+    const uint32_t n = s.light_count;
+    const f3 zero = mk3(0.0f, 0.0f, 0.0f);
+    LightSample ls{zero, sn, zero, 0.0f, false};
+    if (n == 0u) return ls;
+    uint32_t li = f2u_sat(rng_f32(rng) * (float)n);
+    li = li < n ? li : n - 1u;
+    const Light l = load_light(s, li);
+    const float fn = (float)n;
+    if (l.kind == 0u) {
+        f3 to = l.data - hp;
+        float r2 = dot(to, to);
+        float r = sqrtf(r2);
+        f3 ld = to / r;
+        ls.wi = ld;
+        if (dot(sn, ld) <= 0.0f) return ls;
+        f3 pl = mk3(p.ip.point_light_emission[0], p.ip.point_light_emission[1], p.ip.point_light_emission[2]);
+        ls.e = l.color * l.intensity * pl * fmaxf(dot(sn, ld), 0.0f) / (r2 + 0.01f) * fn;
+        ls.o = hp + sn * 0.01f;
+        ls.max_dist = r - 0.001f;
+        ls.occlude = true;
+    } else if (l.kind == 1u) {
+        f3 ld = normalize(l.data);
+        float ndl = dot(sn, ld);
+        ls.wi = ld;
+        if (ndl <= 0.0f) return ls;
+        ls.e = l.color * l.intensity * ndl * fn;
+        ls.o = hp + sn * 0.01f;
+        ls.max_dist = 1e30f;
+        ls.occlude = true;
+    } else if (l.kind == 2u) {
+        TriFull tri = load_tri(s, f2u_sat(l.data.x));
+        Mat mat = load_mat(s, tri.material_id);
+        float u1 = rng_f32(rng);
+        float u2 = rng_f32(rng);
+        float su = sqrtf(u1);
+        float u = 1.0f - su;
+        float v = u2 * su;
+        float w = 1.0f - u - v;
+        f3 lp = tri.v0 * w + tri.v1 * u + tri.v2 * v;
+        float uvx = tri.uv0x * w + tri.uv1x * u + tri.uv2x * v;
+        float uvy = tri.uv0y * w + tri.uv1y * u + tri.uv2y * v;
+        f3 le = l.color;
+        if (mat.tex_emissive != RT_TEX_NONE) {
+            float4 t = tex_sample(s.tex[RT_TEX_EMISSIVE], uvx, uvy, (int32_t)mat.tex_emissive);
+            le = le * mk3(t.x, t.y, t.z);
+        }
+        le = le * mk3(p.ip.light_emission[0], p.ip.light_emission[1], p.ip.light_emission[2]);
+        f3 to = lp - hp;
+        float r2 = dot(to, to);
+        float r = sqrtf(r2);
+        f3 ld = to / r;
+        ls.wi = ld;
+        float ndl = dot(sn, ld);
+        if (ndl <= 0.0f) return ls;
+        f3 ln = triangle_normal(tri.v0, tri.v1, tri.v2);
+        float ndl_l = dot(ln, -ld);
+        if (ndl_l <= 0.0f) return ls;
+        float area = 0.5f * len3(cross(tri.v1 - tri.v0, tri.v2 - tri.v0));
+        ls.e = le * l.intensity * ndl * ndl_l * area * fn / (r2 + 0.01f);
+        ls.o = hp + sn * 0.01f;
+        ls.max_dist = r - 0.001f;
+        ls.occlude = true;
+    }
+    return ls;
+}
+
+__device__ __forceinline__ int32_t clampi(int32_t x, int32_t lo, int32_t hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// The camera ray of the pixel's next sample (gather.wgsl:292-297).
+__device__ __forceinline__ void camera_ray(const WaveParams &p, uint32_t px, uint32_t py, Rng &rng, f3 &ro, f3 &rd) {
+    const rt_camera_uniform &cam = p.cam;
+    float jx = rng_f32(rng) - 0.5f;
+    float jy = rng_f32(rng) - 0.5f;
+    float ux = ((float)px + jx) * cam.inv_half_res[0] - 1.0f;
+    float uy = 1.0f - ((float)py + jy) * cam.inv_half_res[1];
+    ro = mk3(cam.position[0], cam.position[1], cam.position[2]);
+    rd = normalize(mk3(cam.forward[0], cam.forward[1], cam.forward[2]) +
+                   mk3(cam.right[0], cam.right[1], cam.right[2]) * ux + mk3(cam.up[0], cam.up[1], cam.up[2]) * uy);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Appends `item` to queue (count at *counter) for the lanes with want == true; one atomic per warp.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warp_append(bool want, uint32_t item, uint32_t *queue, uint32_t *counter) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (mask == 0u) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (want) queue[base + __popc(mask & lanemask_lt())] = item;
+}
+
+__device__ __forceinline__ uint32_t pack_sb(uint32_t s, uint32_t b) { return (s & 0xFFFFu) | (b << 16); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// generate: 8 x 4 pixel tiles, one per warp, so the first queue is tile-coherent.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant__ WaveParams p) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t tiles_x = (p.ip.width + 7u) / 8u;
+    const uint32_t tile = blockIdx.x * 4u + warp;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    const uint32_t px = tx * 8u + (lane & 7u), py = ty * 4u + (lane >> 3);
+    const bool active = px < p.ip.width && py < p.ip.height;
+    uint32_t pix = 0;
+    if (active) {
+        pix = py * p.ip.width + px;
+        uint32_t base_seed = pix + p.ip.frame * 2654435761u;
+        Rng rng = rng_init(base_seed * 1664525u + 1013904223u);
+        f3 ro, rd;
+        camera_ray(p, px, py, rng, ro, rd);
+        p.ro[pix] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
+        p.rd[pix] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(0u, 0u)));
+        p.thr[pix] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        p.acc[4 * (size_t)pix] = z;
+        p.acc[4 * (size_t)pix + 1] = make_float4(0.0f, 1e30f, 0.0f, 0.0f);
+        p.acc[4 * (size_t)pix + 2] = z;
+        p.acc[4 * (size_t)pix + 3] = z;
+        p.nrm[pix] = make_float4(0.0f, 1.0f, 0.0f, 0.0f);
+    }
+    warp_append(active, pix, p.queue[0], p.counts + 0);
+}
+
+// ------------------------------------------------------------------------------------------------
+// extend: closest hit of each queued path.
+// ------------------------------------------------------------------------------------------------
+template <int kStack>
+__global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+    __shared__ uint32_t stack_smem[kStack * 128];
+    uint32_t *stk = stack_smem + threadIdx.x;
+    const uint32_t n = p.counts[4 * iter];
+    const uint32_t *q = p.queue[iter & 1u];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pix = q[i];
+        const float4 o = p.ro[pix], d = p.rd[pix];
+        Hit h = trace<false>(p.scene, xyz(o), xyz(d), kInf, stk, 128u);
+        p.hit[pix] = make_float2(h.t, __uint_as_float(h.prim));
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// shade: one bounce of gather.wgsl's loop body per queued path.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+    const uint32_t n = p.counts[4 * iter];
+    const uint32_t *q = p.queue[iter & 1u];
+    uint32_t *q_next = p.queue[(iter + 1u) & 1u];
+    uint32_t *n_next = p.counts + 4 * (iter + 1u);
+    uint32_t *n_shadow = p.counts + 4 * iter + 1u;
+    const DevScene &s = p.scene;
+    const rt_image_params &ip = p.ip;
+    const uint32_t W = ip.width;
+    const uint32_t spp = ip.spp > 1u ? ip.spp : 1u;
+    const uint32_t debug_view = ip._pad[0];
+    const float env_intensity = s.env_intensity;
+    const f3 env_color = mk3(s.env_color[0], s.env_color[1], s.env_color[2]);
+    const f3 env_horizon = mk3(s.env_horizon[0], s.env_horizon[1], s.env_horizon[2]);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1u) / stride;
+
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool valid = i < n;
+        bool keep = false;
+        bool emit_shadow = false;
+        uint32_t pix = 0;
+        f3 sh_o = mk3(0.0f, 0.0f, 0.0f), sh_d = sh_o, sh_c = sh_o;
+        float sh_max = 0.0f;
+        uint32_t sh_tag = 0;
+        if (valid) {
+            pix = q[i];
+            const uint32_t px = pix % W, py = pix / W;
+            const float4 o4 = p.ro[pix], d4 = p.rd[pix], t4 = p.thr[pix];
+            const float2 h2 = p.hit[pix];
+            f3 ro = xyz(o4), rd = xyz(d4), thr = xyz(t4);
+            Rng rng{__float_as_uint(o4.w)};
+            const uint32_t sb = __float_as_uint(d4.w);
+            uint32_t sidx = sb & 0xFFFFu, b = sb >> 16;
+            const float hit_t = h2.x;
+            const uint32_t prim = __float_as_uint(h2.y);
+            Accum A = load_acc(p, pix);
+            float4 acc1 = p.acc[4 * (size_t)pix + 1];  // .y = first_depth
+            float4 nrm = p.nrm[pix];
+            bool alive = true;  // the sample continues with another segment
+
+            if (hit_t >= kInf) {
+                if (b > 0u) add_radiance(sidx, A, thr * sky_color(rd, env_color, env_horizon, env_intensity));
+                alive = false;
+            } else {
+                const TriFull tr = load_tri(s, prim);
+                const Mat mat = load_mat(s, tr.material_id);
+                const f3 hp = ro + rd * hit_t;
+                const Bary bb = barycentric(tr, ro, rd, hit_t);
+                const float uvx = bb.uvx, uvy = bb.uvy;
+                bool done_step = false;  // a `continue` of the reference loop
+
+                if ((mat.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && mat.tex_albedo != RT_TEX_NONE &&
+                    tex_sample(s.tex[RT_TEX_ALBEDO], uvx, uvy, (int32_t)mat.tex_albedo).w < 0.5f) {
+                    ro = hp + rd * 0.002f;
+                    done_step = true;
+                }
+                if (!done_step) {
+                    const f3 gn = triangle_normal(tr.v0, tr.v1, tr.v2);
+                    const bool ff = dot(rd, gn) < 0.0f;
+                    const f3 sn_geom = smooth_normal(tr, bb, gn);
+                    const f3 sn = ff ? sn_geom : -sn_geom;
+                    f3 shn = sn;
+                    if (mat.tex_normal != RT_TEX_NONE) {
+                        float4 t = tex_sample(s.tex[RT_TEX_NORMAL], uvx, uvy, (int32_t)mat.tex_normal);
+                        f3 nm = mk3(t.x, t.y, t.z) * 2.0f - mk3(1.0f, 1.0f, 1.0f);
+                        f3 ft, fb;
+                        tangent_frame(tr, sn, ft, fb);
+                        shn = normalize(ft * nm.x + fb * nm.y + sn * nm.z);
+                    }
+                    if (b == 0u && hit_t < acc1.y) {
+                        nrm = make_float4(sn.x, sn.y, sn.z, 0.0f);
+                        acc1.y = hit_t;
+                    }
+                    f3 albedo = mat.albedo;
+                    float rough = mat.roughness, metal = mat.metallic;
+                    if (mat.tex_albedo != RT_TEX_NONE) {
+                        float4 t = tex_sample(s.tex[RT_TEX_ALBEDO], uvx, uvy, (int32_t)mat.tex_albedo);
+                        albedo = mat.albedo * mk3(t.x, t.y, t.z);
+                    }
+                    if (mat.tex_mr != RT_TEX_NONE) {
+                        float4 mr = tex_sample(s.tex[RT_TEX_MR], uvx, uvy, (int32_t)mat.tex_mr);
+                        rough = clampf(mat.roughness * mr.y, 0.0f, 1.0f);
+                        metal = clampf(mat.metallic * mr.z, 0.0f, 1.0f);
+                    }
+                    f3 emis = mat.emissive;
+                    if (mat.tex_emissive != RT_TEX_NONE) {
+                        float4 t = tex_sample(s.tex[RT_TEX_EMISSIVE], uvx, uvy, (int32_t)mat.tex_emissive);
+                        emis = mat.emissive * mk3(t.x, t.y, t.z);
+                    }
+                    add_radiance(sidx, A, thr * emis);
+
+                    bool stop = false;
+                    if (debug_view != 0u) {  // gather.wgsl:359-419
+                        const f3 half = mk3(0.5f, 0.5f, 0.5f);
+                        stop = true;
+                        switch (debug_view) {
+                            case 1: A.col = mk3(uvx, uvy, 0.0f); break;
+                            case 2: A.col = sn * 0.5f + half; break;
+                            case 3: A.col = shn * 0.5f + half; break;
+                            case 4: A.col = gn * 0.5f + half; break;
+                            case 5: A.col = emis; break;
+                            case 8:
+                            case 9: {
+                                float pu = (float)px / (float)ip.width, pv = (float)py / (float)ip.height;
+                                float4 t =
+                                    tex_sample(s.tex[debug_view == 8 ? RT_TEX_EMISSIVE : RT_TEX_ALBEDO], pu, pv, 0);
+                                A.col = mk3(t.x, t.y, t.z);
+                                break;
+                            }
+                            case 11: {
+                                float4 t = tex_sample(s.tex[RT_TEX_EMISSIVE], uvx, uvy, 0);
+                                A.col = mk3(t.x, t.y, t.z);
+                                break;
+                            }
+                            case 12: A.col = mat.emissive; break;
+                            case 13: A.col = mk3((float)mat.tex_emissive / 65535.0f, 0.0f, 0.0f); break;
+                            case 17: A.col = mk3(uvx - floorf(uvx), uvy - floorf(uvy), 0.0f); break;
+                            case 18: {
+                                float4 t = tex_sample(s.tex[RT_TEX_ALBEDO], uvx, uvy, (int32_t)mat.tex_albedo);
+                                A.col = mk3(t.x, t.y, t.z);
+                                break;
+                            }
+                            case 19:
+                            case 20: {
+                                f3 ft, fb;
+                                tangent_frame(tr, sn, ft, fb);
+                                A.col = (debug_view == 19 ? ft : fb) * 0.5f + half;
+                                break;
+                            }
+                            case 21: A.col = hp; break;
+                            default: stop = false; break;
+                        }
+                    }
+                    if (stop) {
+                        alive = false;
+                    } else if (mat.kind == 2u) {  // dielectric (gather.wgsl:421-436)
+                        float qd = (mat.ior - 1.0f) / (mat.ior + 1.0f);
+                        float f0s = powf(qd, 2.0f);
+                        float ct = fabsf(dot(rd, shn));
+                        float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
+                        if (rng_f32(rng) < fr) {
+                            rd = reflect(rd, shn);
+                            ro = hp + shn * 0.001f;
+                        } else {
+                            float eta = ff ? 1.0f / mat.ior : mat.ior;
+                            rd = refract(rd, shn, eta);
+                            ro = hp - shn * 0.001f;
+                            thr = thr * mat.albedo;
+                        }
+                    } else {  // metallic-roughness (gather.wgsl:439-537)
+                        f3 f0 = mk3(0.04f * (1.0f - metal) + albedo.x * metal, 0.04f * (1.0f - metal) + albedo.y * metal,
+                                    0.04f * (1.0f - metal) + albedo.z * metal);
+                        f3 wo = -rd;
+                        float a = fmaxf(rough * rough, 1e-3f);
+                        f3 fr = fresnel_schlick(fabsf(dot(rd, shn)), f0);
+                        f3 diffuse_weight = (1.0f - metal) * albedo;
+                        float sp = max3(fr);
+                        float dp = max3(diffuse_weight);
+                        float ratio = sp / (sp + dp);
+                        float spec_prob = clampf(sp + dp <= 0.0f ? 0.5f : ratio, 0.001f, 0.999f);
+                        bool do_spec = rng_f32(rng) < spec_prob;
+                        f3 dscale = diffuse_weight / (1.0f - spec_prob);
+
+                        LightSample ls = light_sample(p, hp, shn, rng);
+                        f3 c_nee;
+                        if (!do_spec) {
+                            if (env_intensity > 0.0f)
+                                add_radiance(sidx, A, thr * dscale * sky_color(shn, env_color, env_horizon, env_intensity));
+                            c_nee = thr * dscale * ls.e / kPi;
+                            add_radiance(sidx, A, thr * albedo * ip.ambient);
+                        } else {
+                            c_nee = thr * spec_ggx(wo, shn, ls.wi, a, f0) * ls.e / spec_prob;
+                        }
+                        bool nee_luma_only = false;
+                        if (ip.use_photons == 1u && !do_spec) {  // gather.wgsl:473-514
+                            const rt_grid_params &gp = p.gp;
+                            float r2 = ip.photon_radius * ip.photon_radius;
+                            f3 ph_sum = mk3(0.0f, 0.0f, 0.0f);
+                            uint32_t ph_hits = 0u, budget = 384u;
+                            bool done = false;
+                            int32_t bx = f2i_sat((hp.x - gp.room_min_x) / gp.cell_size);
+                            int32_t by = f2i_sat((hp.y - gp.room_min_y) / gp.cell_size);
+                            int32_t bz = f2i_sat((hp.z - gp.room_min_z) / gp.cell_size);
+                            int32_t gxmax = (int32_t)gp.grid_x - 1, gymax = (int32_t)gp.grid_y - 1,
+                                    gzmax = (int32_t)gp.grid_z - 1;
+                            for (int32_t dz = -1; dz <= 1 && !done; ++dz)
+                                for (int32_t dy = -1; dy <= 1 && !done; ++dy)
+                                    for (int32_t dx = -1; dx <= 1 && !done; ++dx) {
+                                        int32_t cx = clampi((int32_t)((uint32_t)bx + (uint32_t)dx), 0, gxmax);
+                                        int32_t cy = clampi((int32_t)((uint32_t)by + (uint32_t)dy), 0, gymax);
+                                        int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
+                                        uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x +
+                                                        (uint32_t)cz * gp.grid_x * gp.grid_y;
+                                        uint2 m = __ldg(p.grid_meta + cell);
+                                        for (uint32_t k = 0; k < m.y && !done; ++k) {
+                                            if (budget == 0u) {
+                                                done = true;
+                                                break;
+                                            }
+                                            budget -= 1u;
+                                            uint64_t idx = (uint64_t)m.x + k;
+                                            idx = idx < p.sorted_count ? idx : p.sorted_count - 1;
+                                            const float4 *ph = p.sorted_photons + 4ull * idx;
+                                            f3 dd = xyz(__ldg(ph)) - hp;
+                                            float d2 = dot(dd, dd);
+                                            if (d2 < r2) {
+                                                f3 pw = xyz(__ldg(ph + 1));
+                                                f3 inc = xyz(__ldg(ph + 2));
+                                                ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
+                                                ph_hits += 1u;
+                                                if (ph_hits >= 64u) {
+                                                    done = true;
+                                                    break;
+                                                }
+                                            }
+                                        }
+                                    }
+                            if (ph_hits > 0u)
+                                add_radiance(sidx, A,
+                                             thr * dscale * ph_sum * ip.photon_scale /
+                                                 (kPi * (float)ph_hits * ip.photon_radius * ip.photon_radius));
+                            if (ip.photon_debug == 1u) {
+                                float density = fminf((float)ph_hits / 64.0f, 1.0f);
+                                A.col = mk3(1.0f - density, density, 0.0f) * 2.0f;
+                                nee_luma_only = true;  // the reference added the NEE term before this overwrite
+                            }
+                        }
+                        if (ls.occlude && (c_nee.x != 0.0f || c_nee.y != 0.0f || c_nee.z != 0.0f)) {
+                            emit_shadow = true;
+                            sh_o = ls.o;
+                            sh_d = ls.wi;
+                            sh_c = c_nee;
+                            sh_max = ls.max_dist;
+                            sh_tag = (sidx & 0xFFFFu) | (nee_luma_only ? 0x10000u : 0u);
+                        }
+                        if (do_spec) {
+                            rd = sample_spec_dir(rd, shn, a, rng);
+                            ro = hp + shn * 0.001f;
+                            f3 h = normalize(wo + rd);
+                            float ndl = fmaxf(dot(shn, rd), 0.0f);
+                            thr = thr * fresnel_schlick(fmaxf(dot(wo, h), 0.0f), f0) * smith_g1(ndl, a) / spec_prob;
+                        } else {
+                            f3 local = sample_cosine_hemisphere(rng);
+                            rd = to_world(local, shn);
+                            ro = hp + shn * 0.001f;
+                            thr = thr * dscale;
+                            if (ip.use_photons == 1u) alive = false;
+                        }
+                        if (alive) {
+                            float pr = max3(thr);
+                            if (pr <= 0.0f || rng_f32(rng) > pr) alive = false;
+                            else thr = thr / pr;
+                        }
+                    }
+                }
+            }
+            // for-loop step: the segment index advances; the sample ends after max_bounces segments.
+            b += 1u;
+            if (alive && b >= p.max_bounces) alive = false;
+            if (!alive) {
+                sidx += 1u;
+                if (sidx < spp) {
+                    camera_ray(p, px, py, rng, ro, rd);
+                    thr = mk3(1.0f, 1.0f, 1.0f);
+                    b = 0u;
+                    keep = true;
+                }
+            } else {
+                keep = true;
+            }
+            p.ro[pix] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
+            p.rd[pix] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(sidx, b)));
+            p.thr[pix] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+            store_acc(p, pix, A, acc1);
+            p.nrm[pix] = nrm;
+        }
+        // NEE shadow ray (deferred) and the continuing path.
+        {
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, emit_shadow);
+            if (mask) {
+                const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(n_shadow, (uint32_t)__popc(mask));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (emit_shadow) {
+                    float4 *rec = p.shadow + 3ull * (base + __popc(mask & lanemask_lt()));
+                    rec[0] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_max);
+                    rec[1] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(pix));
+                    rec[2] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sh_tag));
+                }
+            }
+        }
+        warp_append(keep, pix, q_next, n_next);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// shadow: the deferred NEE occlusion test (gather.wgsl:91-103) and the contribution of visible lights.
+// ------------------------------------------------------------------------------------------------
+template <int kStack>
+__global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+    __shared__ uint32_t stack_smem[kStack * 128];
+    uint32_t *stk = stack_smem + threadIdx.x;
+    const uint32_t m = p.counts[4 * iter + 1];
+    const DevScene &s = p.scene;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const float4 *rec = p.shadow + 3ull * i;
+        const float4 o = rec[0], d = rec[1], c = rec[2];
+        const f3 origin = xyz(o), dir = xyz(d);
+        const float limit = o.w - 0.001f;
+        bool shadowed;
+        if (s.any_hit_shadows) {
+            shadowed = trace<true>(s, origin, dir, limit, stk, 128u).t < kInf;
+        } else {
+            Hit sh = trace<false>(s, origin, dir, kInf, stk, 128u);
+            shadowed = !(sh.t >= limit);
+            if (shadowed) {
+                TriFull bt = load_tri(s, sh.prim);
+                Mat bm = load_mat(s, bt.material_id);
+                if ((bm.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && bm.tex_albedo != RT_TEX_NONE) {
+                    Bary b = barycentric(bt, origin, dir, sh.t);
+                    if (tex_sample(s.tex[RT_TEX_ALBEDO], b.uvx, b.uvy, (int32_t)bm.tex_albedo).w < 0.5f) shadowed = false;
+                }
+            }
+        }
+        if (shadowed) continue;
+        const uint32_t pix = __float_as_uint(d.w);
+        const uint32_t tag = __float_as_uint(c.w);
+        Accum A = load_acc(p, pix);
+        const float4 acc1 = p.acc[4 * (size_t)pix + 1];
+        if (tag & 0x10000u) add_luma(tag & 0xFFFFu, A, xyz(c));
+        else add_radiance(tag & 0xFFFFu, A, xyz(c));
+        store_acc(p, pix, A, acc1);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// finalize: firefly sigma clamp and the frame outputs (gather.wgsl:548-593); segment counters.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant__ WaveParams p, uint32_t iters) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix == 0u && p.counters) {
+        unsigned long long seg = 0, shd = 0;
+        for (uint32_t i = 0; i < iters; ++i) {
+            seg += p.counts[4 * i];
+            shd += p.counts[4 * i + 1];
+        }
+        atomicAdd(p.counters + 0, seg);
+        atomicAdd(p.counters + 1, shd);
+    }
+    if (pix >= p.npix) return;
+    const uint32_t spp = p.ip.spp > 1u ? p.ip.spp : 1u;
+    Accum A = load_acc(p, pix);
+    const float first_depth = p.acc[4 * (size_t)pix + 1].y;
+    const float4 nrm = p.nrm[pix];
+    if (spp <= 8u) {
+        float *sl = A.sl;
+        for (uint32_t i = 1; i < spp; ++i) {
+            float key = sl[i];
+            uint32_t j = i;
+            while (j > 0u && sl[j - 1u] > key) {
+                sl[j] = sl[j - 1u];
+                j -= 1u;
+            }
+            sl[j] = key;
+        }
+        float median = (sl[(spp - 1u) / 2u] + sl[spp / 2u]) * 0.5f;
+        uint32_t half = spp / 2u > 1u ? spp / 2u : 1u;
+        float spread = 0.0f;
+        for (uint32_t i = 0; i < half; ++i) {
+            float dd = sl[i] - median;
+            spread += dd * dd;
+        }
+        float sigma = fmaxf(sqrtf(spread / (float)half), 0.25f * median + 1e-5f);
+        float thresh = median + 3.0f * sigma;
+        float cl = 0.0f, cl2 = 0.0f;
+        for (uint32_t i = 0; i < spp; ++i) {
+            float lc = fminf(sl[i], thresh);
+            cl += lc;
+            cl2 += lc * lc;
+        }
+        A.col = A.col * (cl / fmaxf(A.lum_sum, 1e-10f));
+        A.lum_sum = cl;
+        A.lum2_sum = cl2;
+    }
+    f3 col = vmin(A.col / (float)spp, mk3(10.0f, 10.0f, 10.0f));
+    p.frame[pix] = make_float4(col.x, col.y, col.z, 1.0f);
+    p.moments[pix] = make_float4(fminf(A.lum_sum / (float)spp, 10.0f), fminf(A.lum2_sum / (float)spp, 100.0f), 0.0f, 0.0f);
+    p.gbuffer[pix] = make_float4(nrm.x, nrm.y, nrm.z, first_depth);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host launcher: the whole gather pass of one frame.
+// ------------------------------------------------------------------------------------------------
+cudaError_t launch_wavefront(const WaveParams &p, uint32_t iters, int num_sms, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4 * (size_t)(iters + 1), st)) != cudaSuccess) return e;
+    const uint32_t tiles = ((p.ip.width + 7u) / 8u) * ((p.ip.height + 3u) / 4u);
+    wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p);
+    const uint32_t blocks_needed = (p.npix + 127u) / 128u;
+    const uint32_t persistent = (uint32_t)num_sms * 8u;
+    const uint32_t grid = blocks_needed < persistent ? blocks_needed : persistent;
+    const bool big_stack = p.scene.stack_cap > 32u;
+    for (uint32_t it = 0; it < iters; ++it) {
+        if (big_stack) wf_extend_kernel<64><<<grid, 128, 0, st>>>(p, it);
+        else wf_extend_kernel<32><<<grid, 128, 0, st>>>(p, it);
+        wf_shade_kernel<<<grid, 128, 0, st>>>(p, it);
+        if (big_stack) wf_shadow_kernel<64><<<grid, 128, 0, st>>>(p, it);
+        else wf_shadow_kernel<32><<<grid, 128, 0, st>>>(p, it);
+    }
+    wf_finalize_kernel<<<(p.npix + 255u) / 256u, 256, 0, st>>>(p, iters);
+    return cudaGetLastError();
+}
+
+}  // namespace rtd

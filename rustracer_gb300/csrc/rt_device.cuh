@@ -115,12 +115,21 @@ struct DevTex {
 };
 
 struct DevScene {
-    const float4 *nodes;     // 3 x float4 per BVHNode
-    const uint32_t *prims;
+    // Traversal layout, derived at create from the reference's BVHNode / prim-index / triangle arrays
+    // (same tree): one 64-byte record per internal node holding both children's boxes
+    //   q0 = (left.min, left.ref)  q1 = (left.max, left.count)  q2 = (right.min, right.ref)
+    //   q3 = (right.max, right.count)
+    // where count > 0 marks a leaf child (ref = first slot in the leaf-ordered triangles) and
+    // count == 0 an internal child (ref = its record index); and one 48-byte record per prim slot,
+    // (v0, original index), (v1 - v0), (v2 - v0): the edges Moller-Trumbore computes first.
+    const float4 *cnodes;
+    const float4 *tri_ord;
+    uint32_t cnode_count, stack_cap;
+    uint32_t any_hit_shadows;  // 1: no alpha-cutout material, shadow rays may stop at the first hit
     const float4 *tris;      // 8 x float4 per TriangleGpu
     const float4 *mats;      // 4 x float4 per MaterialGpu
     const float4 *lights;    // 4 x float4 per LightGpu
-    uint32_t node_count, prim_count, tri_count, mat_count, light_count;
+    uint32_t tri_count, mat_count, light_count;
     DevTex tex[4];
     // The first environment light (gather.wgsl:276-289), resolved on the host.
     float env_intensity;
@@ -248,54 +257,91 @@ struct Hit {
     uint32_t prim;
 };
 
-// Closest hit by the reference's traversal (gather.wgsl:66-88): 64-entry stack, left child first,
-// right child pushed (dropped when 63 entries are in use), every primitive of a visited leaf tested,
-// first strictly-smaller t wins.  The stack lives in shared memory, one column per thread.
-template <int kStack>
-__device__ __forceinline__ Hit trace_bvh(const DevScene &s, f3 ro, f3 rd, uint32_t *stk, uint32_t stride) {
-    Hit hit{kInf, 0u};
-    if (s.node_count == 0u) return hit;
-    f3 inv = mk3(1.0f, 1.0f, 1.0f) / rd;
-    uint32_t idx = 0u, sp = 0u;
+// BVH traversal over the child-pair records.  Each record fetch tests both children's boxes with the
+// reference's slab test (gather.wgsl:71-75: (bmin - ro) / d, te <= ta && ta > 0 && te < t); leaf
+// children are intersected on the spot, internal children are visited nearest entry first with the
+// farther one pushed (a push is dropped once `cap` entries are in use, as the reference drops pushes
+// at 63).  The tree is the reference's, so the closest hit is the reference's: only triangles with
+// exactly equal t may resolve to a different one of them.  The stack lives in shared memory, one
+// 4-byte column per thread.
+//
+// kAny: stop at the first triangle with t < t_limit (occlusion query); otherwise the closest hit below
+// t_limit.
+template <bool kAny>
+__device__ __forceinline__ Hit trace(const DevScene &s, f3 ro, f3 rd, float t_limit, uint32_t *stk,
+                                     uint32_t stride) {
+    Hit hit{t_limit, 0u};
+    if (s.cnode_count == 0u) return Hit{kInf, 0u};
+    const f3 inv = mk3(1.0f, 1.0f, 1.0f) / rd;
+    const uint32_t cap = s.stack_cap;
+    uint32_t node = 0u, sp = 0u;
     for (;;) {
-        const float4 *np = s.nodes + 3ull * clampi_u(idx, s.node_count);
-        float4 a = __ldg(np), b = __ldg(np + 1);
-        uint32_t pc = __ldg(reinterpret_cast<const uint32_t *>(np + 2));
-        f3 t0 = (xyz(a) - ro) * inv;
-        f3 t1 = (xyz(b) - ro) * inv;
-        f3 tm = vmin(t0, t1);
-        f3 tx = vmax(t0, t1);
-        float te = fmaxf(fmaxf(tm.x, tm.y), tm.z);
-        float ta = fminf(fminf(tx.x, tx.y), tx.z);
-        if (te <= ta && ta > 0.0f && te < hit.t) {
-            uint32_t lf = __float_as_uint(a.w);
-            if (pc > 0u) {
-                for (uint32_t i = 0; i < pc; ++i) {
-                    uint32_t slot = clampi_u(lf + i, s.prim_count);
-                    uint32_t pi = __ldg(s.prims + slot);
-                    Tri tr = load_tri_verts(s, pi);
-                    float t = intersect_triangle(ro, rd, tr.v0, tr.v1, tr.v2);
+        const float4 *np = s.cnodes + 4ull * node;
+        const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
+        f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
+        const float le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
+        const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
+        const float re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
+        const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
+        bool hl = le <= lx && lx > 0.0f && le < hit.t;
+        bool hr = re <= rx && rx > 0.0f && re < hit.t;
+        const uint32_t lref = __float_as_uint(q0.w), lcnt = __float_as_uint(q1.w);
+        const uint32_t rref = __float_as_uint(q2.w), rcnt = __float_as_uint(q3.w);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const bool h = side == 0 ? hl : hr;
+            const uint32_t cnt = side == 0 ? lcnt : rcnt;
+            if (h && cnt) {
+                const uint32_t first = side == 0 ? lref : rref;
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    const float4 *tp = s.tri_ord + 3ull * (first + k);
+                    const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+                    const f3 h3 = cross(rd, xyz(e2));
+                    const float a = dot(xyz(e1), h3);
+                    float t = kInf;
+                    if (!(fabsf(a) < 1e-7f)) {
+                        const float f = 1.0f / a;
+                        const f3 sv = ro - xyz(v0);
+                        const float u = f * dot(sv, h3);
+                        if (!(u < 0.0f || u > 1.0f)) {
+                            const f3 q = cross(sv, xyz(e1));
+                            const float v = f * dot(rd, q);
+                            if (!(v < 0.0f || u + v > 1.0f)) {
+                                const float tt = f * dot(xyz(e2), q);
+                                if (tt > kEps) t = tt;
+                            }
+                        }
+                    }
                     if (t < hit.t) {
                         hit.t = t;
-                        hit.prim = pi;
+                        hit.prim = __float_as_uint(v0.w);
+                        if (kAny) return hit;
                     }
                 }
-                if (sp == 0u) break;
-                sp -= 1u;
-                idx = stk[sp * stride];
-            } else {
-                if (sp < (uint32_t)(kStack - 1)) {
-                    stk[sp * stride] = __float_as_uint(b.w);
-                    sp += 1u;
-                }
-                idx = lf;
+                if (side == 0) hl = false;
+                else hr = false;
             }
+        }
+        if (hl && hr) {
+            const bool left_first = le <= re;
+            const uint32_t far = left_first ? rref : lref;
+            node = left_first ? lref : rref;
+            if (sp < cap) {
+                stk[sp * stride] = far;
+                sp += 1u;
+            }
+        } else if (hl) {
+            node = lref;
+        } else if (hr) {
+            node = rref;
         } else {
             if (sp == 0u) break;
             sp -= 1u;
-            idx = stk[sp * stride];
+            node = stk[sp * stride];
         }
     }
+    if (kAny) hit.t = kInf;  // nothing closer than the limit
     return hit;
 }
 

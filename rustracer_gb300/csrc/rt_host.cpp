@@ -211,6 +211,109 @@ BVH build_bvh(const std::vector<Vec3> &centroids, const std::vector<Vec3> &bmin,
 }
 
 // ------------------------------------------------------------------------------------------------
+// Traversal layout (child-pair records over the reference's tree)
+// ------------------------------------------------------------------------------------------------
+static inline uint32_t f2bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+static inline float bits2f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+bool build_traversal_layout(const rt_bvh_node *nodes, uint64_t n_nodes, const uint32_t *prims, uint64_t n_prims,
+                            const rt_triangle *tris, uint64_t n_tris, TraversalLayout &out) {
+    out.cnodes.clear();
+    out.tri_ord.clear();
+    out.max_depth = 0;
+    if (n_nodes == 0) return true;
+    // Leaf-ordered triangles: slot k holds triangle prims[k] with its two edges precomputed.
+    out.tri_ord.resize(n_prims * 12);
+    for (uint64_t k = 0; k < n_prims; ++k) {
+        uint32_t id = prims[k];
+        if (id >= n_tris) {
+            set_error("BVH prim slot %llu references triangle %u of %llu", (unsigned long long)k, id,
+                      (unsigned long long)n_tris);
+            return false;
+        }
+        const rt_triangle &t = tris[id];
+        float *o = &out.tri_ord[k * 12];
+        o[0] = t.v0[0]; o[1] = t.v0[1]; o[2] = t.v0[2]; o[3] = bits2f(id);
+        o[4] = t.v1[0] - t.v0[0]; o[5] = t.v1[1] - t.v0[1]; o[6] = t.v1[2] - t.v0[2]; o[7] = 0.0f;
+        o[8] = t.v2[0] - t.v0[0]; o[9] = t.v2[1] - t.v0[1]; o[10] = t.v2[2] - t.v0[2]; o[11] = 0.0f;
+    }
+    auto leaf_ok = [&](const rt_bvh_node &n) { return (uint64_t)n.left_first + n.prim_count <= n_prims; };
+    // Record index of every internal node, in node order (the root, node 0, gets record 0).
+    std::vector<uint32_t> rec(n_nodes, 0xFFFFFFFFu);
+    uint32_t n_int = 0;
+    for (uint64_t i = 0; i < n_nodes; ++i)
+        if (nodes[i].prim_count == 0) rec[i] = n_int++;
+    auto child = [&](uint32_t c, float *box_lo, float *box_hi, uint32_t *ref, uint32_t *cnt) -> bool {
+        if (c >= n_nodes) {
+            set_error("BVH child index %u out of range (%llu nodes)", c, (unsigned long long)n_nodes);
+            return false;
+        }
+        const rt_bvh_node &n = nodes[c];
+        for (int a = 0; a < 3; ++a) {
+            box_lo[a] = n.bbox_min[a];
+            box_hi[a] = n.bbox_max[a];
+        }
+        if (n.prim_count > 0) {
+            if (!leaf_ok(n)) {
+                set_error("BVH leaf %u exceeds the prim-index array", c);
+                return false;
+            }
+            *ref = n.left_first;
+            *cnt = n.prim_count;
+        } else {
+            *ref = rec[c];
+            *cnt = 0;
+        }
+        return true;
+    };
+    auto emit = [&](uint32_t l, uint32_t r) -> bool {
+        float q[16];
+        uint32_t lref, lcnt, rref, rcnt;
+        if (!child(l, &q[0], &q[4], &lref, &lcnt) || !child(r, &q[8], &q[12], &rref, &rcnt)) return false;
+        q[3] = bits2f(lref);
+        q[7] = bits2f(lcnt);
+        q[11] = bits2f(rref);
+        q[15] = bits2f(rcnt);
+        out.cnodes.insert(out.cnodes.end(), q, q + 16);
+        return true;
+    };
+    if (nodes[0].prim_count > 0) {  // single-leaf tree: both children are the root leaf
+        if (!emit(0, 0)) return false;
+        out.max_depth = 0;
+        return true;
+    }
+    out.cnodes.reserve((size_t)n_int * 16);
+    for (uint64_t i = 0; i < n_nodes; ++i)
+        if (nodes[i].prim_count == 0 && !emit(nodes[i].left_first, nodes[i].right_child)) return false;
+    // Depth (iterative; also rejects cycles by bounding the walk to n_nodes visits).
+    std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
+    uint64_t visits = 0;
+    while (!st.empty()) {
+        auto [i, d] = st.back();
+        st.pop_back();
+        if (++visits > n_nodes) {
+            set_error("BVH is not a tree (a node is reachable twice)");
+            return false;
+        }
+        out.max_depth = std::max(out.max_depth, d);
+        if (nodes[i].prim_count == 0) {
+            st.push_back({nodes[i].left_first, d + 1});
+            st.push_back({nodes[i].right_child, d + 1});
+        }
+    }
+    (void)f2bits;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------
 // Deterministic host RNG for the procedural scenes (splitmix64; Irwin-Hall normal approximation).
 // Only integer arithmetic and +,-,*,/ so both host architectures build identical scenes.
 // ------------------------------------------------------------------------------------------------

@@ -53,6 +53,18 @@ struct BVH {
 // BVHBuilder::build (rustracer-core/src/bvh.rs:135-336).
 BVH build_bvh(const std::vector<Vec3> &centroids, const std::vector<Vec3> &bmin, const std::vector<Vec3> &bmax);
 
+// The traversal layout of the device kernels, derived from the reference's arrays (same tree):
+// 16 floats per internal node (both children's boxes, refs and leaf counts) and 12 floats per prim
+// slot ((v0, original index), v1 - v0, v2 - v0).  A tree that is a single leaf gets one record whose
+// two children are that leaf.  Returns false (with the error set) on an inconsistent input.
+struct TraversalLayout {
+    std::vector<float> cnodes;   // 16 per record
+    std::vector<float> tri_ord;  // 12 per prim slot
+    uint32_t max_depth = 0;      // root-to-leaf edges of the deepest leaf
+};
+bool build_traversal_layout(const rt_bvh_node *nodes, uint64_t n_nodes, const uint32_t *prims, uint64_t n_prims,
+                            const rt_triangle *tris, uint64_t n_tris, TraversalLayout &out);
+
 }  // namespace rt
 
 struct rt_scene {

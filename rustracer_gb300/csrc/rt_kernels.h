@@ -8,7 +8,8 @@
 
 namespace rtd {
 
-struct GatherParams {
+// The wavefront gather pass.  Path state has one slot per pixel (slot == pixel index).
+struct WaveParams {
     DevScene scene;
     rt_camera_uniform cam;
     rt_image_params ip;
@@ -16,13 +17,24 @@ struct GatherParams {
     const float4 *sorted_photons;  // 4 x float4 per photon
     uint64_t sorted_count;
     const uint2 *grid_meta;        // (start, count) per cell
-    uint32_t max_bounces;
+    uint32_t max_bounces, npix;
+    float4 *ro;        // origin, .w = RNG state
+    float4 *rd;        // direction, .w = sample index | segment index << 16
+    float4 *thr;       // throughput
+    float2 *hit;       // closest t, primitive
+    float4 *acc;       // 4 per pixel: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
+    float4 *nrm;       // first-hit shading normal
+    uint32_t *queue[2];
+    uint32_t *counts;  // per iteration: [0] paths queued, [1] shadow rays
+    float4 *shadow;    // 3 per deferred NEE ray: (origin, max_dist), (dir, pixel), (contribution, tag)
     float4 *frame;
     float4 *moments;
     float4 *gbuffer;
-    unsigned long long *counters;  // [0] segments, [1] shadow rays
+    unsigned long long *counters;  // [0] segments, [1] shadow rays (cumulative)
 };
-__global__ void gather_kernel(const __grid_constant__ GatherParams p);
+// generate, spp * max_bounces iterations of extend / shade / shadow, finalize.
+cudaError_t launch_wavefront(const WaveParams &p, uint32_t iters, int num_sms, cudaStream_t st);
+int device_sm_count();
 
 struct PhotonTraceParams {
     DevScene scene;
@@ -35,7 +47,6 @@ struct PhotonTraceParams {
 __global__ void photon_trace_kernel(const __grid_constant__ PhotonTraceParams p);
 
 // Launchers (stream-ordered, no synchronisation).  Each returns the launch error, if any.
-cudaError_t launch_gather(const GatherParams &p, cudaStream_t st);
 cudaError_t launch_photon_trace(const PhotonTraceParams &p, cudaStream_t st);
 
 // Photon grid (exact u32 counting sort).  Scratch sizes come from grid_scratch_bytes.

@@ -2,8 +2,11 @@
 // frame schedule of rustracer-renderer's Renderer (rustracer-renderer/src/lib.rs:227-1042).
 //
 // HBM layout per renderer (all cudaMalloc'd at create, freed at destroy):
-//   scene:  triangles 128 B, BVH nodes 48 B, prim indices 4 B, materials 64 B, lights 64 B (AoS, the
-//           reference layouts); role textures as rgba8 arrays (layer-major).
+//   scene:  triangles 128 B, materials 64 B, lights 64 B (AoS, the reference layouts); role textures
+//           as rgba8 arrays (layer-major); the traversal layout derived from the reference's BVH:
+//           one 64 B record per internal node, one 48 B leaf-ordered triangle record per prim slot.
+//   path:   per pixel, origin / direction / throughput (16 B each), hit 8 B, accumulators 64 B,
+//           first normal 16 B, two queue entries 4 B, one deferred shadow ray 48 B (192 B / pixel).
 //   frame:  frame, denoise ping-pong, moments, gbuffer, accumulation (float4 per pixel each) and the
 //           rgba8 output image.
 //   photon: photon slots (64 B, 6 per photon), u32 key per slot, slot order, sorted photons (64 B),
@@ -107,8 +110,12 @@ struct rt_renderer {
     rt_camera_uniform cam{};
     std::vector<rt_light> lights_host;
     rtd::DevScene scene{};
-    DevBuf d_nodes, d_prims, d_tris, d_mats, d_lights, d_tex[4];
+    DevBuf d_cnodes, d_tri_ord, d_tris, d_mats, d_lights, d_tex[4];
     DevBuf d_frame, d_pingpong, d_moments, d_gbuffer, d_accum, d_output;
+    // wavefront path state (one slot per pixel)
+    DevBuf w_ro, w_rd, w_thr, w_hit, w_acc, w_nrm, w_queue[2], w_shadow, w_counts;
+    size_t w_counts_bytes = 0;
+    int num_sms = 1;
     DevBuf d_photons, d_keys, d_order, d_sorted, d_counts, d_meta, d_cursor, d_partials, d_total, d_counters;
     uint64_t photon_slots = 1;
     bool photon_buffers = false;
@@ -258,19 +265,30 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
 
     // Scene upload (Renderer::new, lib.rs:234-266).
     if ((st = upload(r->d_tris, sd->triangles, sd->triangle_count, s)) != RT_OK) return fail(st);
-    if ((st = upload(r->d_nodes, sd->bvh_nodes, sd->bvh_node_count, s)) != RT_OK) return fail(st);
-    if ((st = upload(r->d_prims, sd->bvh_prims, sd->bvh_prim_count, s)) != RT_OK) return fail(st);
+    rt::TraversalLayout lay;
+    if (!rt::build_traversal_layout(sd->bvh_nodes, sd->bvh_node_count, sd->bvh_prims, sd->bvh_prim_count,
+                                    sd->triangles, sd->triangle_count, lay))
+        return fail(RT_ERR_INVALID_ARGUMENT);
+    if ((st = upload(r->d_cnodes, lay.cnodes.data(), lay.cnodes.size(), s)) != RT_OK) return fail(st);
+    if ((st = upload(r->d_tri_ord, lay.tri_ord.data(), lay.tri_ord.size(), s)) != RT_OK) return fail(st);
+    // Host copies of the layout are freed when `lay` goes out of scope; wait for the copies first.
+    RT_CK(cudaStreamSynchronize(s));
     if ((st = upload(r->d_mats, sd->materials, sd->material_count, s)) != RT_OK) return fail(st);
     if ((st = upload(r->d_lights, sd->lights, sd->light_count, s)) != RT_OK) return fail(st);
     r->lights_host.assign(sd->lights, sd->lights + sd->light_count);
     rtd::DevScene &ds = r->scene;
-    ds.nodes = r->d_nodes.as<float4>();
-    ds.prims = r->d_prims.as<uint32_t>();
+    ds.cnodes = r->d_cnodes.as<float4>();
+    ds.tri_ord = r->d_tri_ord.as<float4>();
+    ds.cnode_count = (uint32_t)(lay.cnodes.size() / 16);
+    // A near-first traversal holds at most one pending entry per tree level.
+    ds.stack_cap = lay.max_depth < 32u ? 32u : 63u;
+    ds.any_hit_shadows = 1u;
+    for (uint64_t i = 0; i < sd->material_count; ++i)
+        if ((sd->materials[i].flags & RT_MAT_FLAG_ALPHA_CUTOUT) && sd->materials[i].tex_albedo != RT_TEX_NONE)
+            ds.any_hit_shadows = 0u;
     ds.tris = r->d_tris.as<float4>();
     ds.mats = r->d_mats.as<float4>();
     ds.lights = r->d_lights.as<float4>();
-    ds.node_count = (uint32_t)sd->bvh_node_count;
-    ds.prim_count = (uint32_t)sd->bvh_prim_count;
     ds.tri_count = (uint32_t)sd->triangle_count;
     ds.mat_count = (uint32_t)sd->material_count;
     ds.light_count = (uint32_t)sd->light_count;
@@ -302,6 +320,21 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
         }
         RT_CK(cudaMemsetAsync(b->p, 0, npix * 16, s));
     }
+    {
+        DevBuf *wb[6] = {&r->w_ro, &r->w_rd, &r->w_thr, &r->w_nrm, &r->w_hit, &r->w_acc};
+        const size_t wsz[6] = {16, 16, 16, 16, 8, 64};
+        for (int i = 0; i < 6; ++i)
+            if (wb[i]->alloc(npix * wsz[i]) != cudaSuccess) {
+                set_error("rt_renderer_create: out of device memory for path state");
+                return fail(RT_ERR_OUT_OF_MEMORY);
+            }
+        if (r->w_queue[0].alloc(npix * 4) != cudaSuccess || r->w_queue[1].alloc(npix * 4) != cudaSuccess ||
+            r->w_shadow.alloc(npix * 48) != cudaSuccess) {
+            set_error("rt_renderer_create: out of device memory for ray queues");
+            return fail(RT_ERR_OUT_OF_MEMORY);
+        }
+    }
+    r->num_sms = rtd::device_sm_count();
     RT_CK(r->d_output.alloc(npix * 4));
     RT_CK(cudaMemsetAsync(r->d_output.p, 0, npix * 4, s));
     RT_CK(r->d_counters.alloc(64));
@@ -358,21 +391,40 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     for (auto &e : fe) RT_CK(r->ring.next(&e));
     RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
-    rtd::GatherParams gp;
-    std::memset(&gp, 0, sizeof(gp));
-    gp.scene = r->scene;
-    gp.cam = r->cam;
-    gp.ip = image_params(r, alpha);
-    gp.gp = r->gp;
-    gp.sorted_photons = r->d_sorted.as<float4>();
-    gp.sorted_count = r->photon_slots;
-    gp.grid_meta = r->d_meta.as<uint2>();
-    gp.max_bounces = max_bounces(c);
-    gp.frame = r->d_frame.as<float4>();
-    gp.moments = r->d_moments.as<float4>();
-    gp.gbuffer = r->d_gbuffer.as<float4>();
-    gp.counters = r->d_counters.as<unsigned long long>();
-    RT_CK(rtd::launch_gather(gp, s));
+    const uint32_t spp = c.spp > 1u ? c.spp : 1u;
+    const uint32_t iters = spp * max_bounces(c);
+    const size_t counts_bytes = sizeof(uint32_t) * 4 * ((size_t)iters + 1);
+    if (counts_bytes > r->w_counts_bytes) {
+        RT_CK(cudaStreamSynchronize(s));
+        RT_CK(r->w_counts.alloc(counts_bytes));
+        r->w_counts_bytes = counts_bytes;
+    }
+    rtd::WaveParams wp;
+    std::memset(&wp, 0, sizeof(wp));
+    wp.scene = r->scene;
+    wp.cam = r->cam;
+    wp.ip = image_params(r, alpha);
+    wp.gp = r->gp;
+    wp.sorted_photons = r->d_sorted.as<float4>();
+    wp.sorted_count = r->photon_slots;
+    wp.grid_meta = r->d_meta.as<uint2>();
+    wp.max_bounces = max_bounces(c);
+    wp.npix = (uint32_t)npix;
+    wp.ro = r->w_ro.as<float4>();
+    wp.rd = r->w_rd.as<float4>();
+    wp.thr = r->w_thr.as<float4>();
+    wp.hit = r->w_hit.as<float2>();
+    wp.acc = r->w_acc.as<float4>();
+    wp.nrm = r->w_nrm.as<float4>();
+    wp.queue[0] = r->w_queue[0].as<uint32_t>();
+    wp.queue[1] = r->w_queue[1].as<uint32_t>();
+    wp.counts = r->w_counts.as<uint32_t>();
+    wp.shadow = r->w_shadow.as<float4>();
+    wp.frame = r->d_frame.as<float4>();
+    wp.moments = r->d_moments.as<float4>();
+    wp.gbuffer = r->d_gbuffer.as<float4>();
+    wp.counters = r->d_counters.as<unsigned long long>();
+    RT_CK(rtd::launch_wavefront(wp, iters, r->num_sms, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
 
@@ -806,14 +858,3 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     return RT_OK;
 }
 
-// ------------------------------------------------------------------------------------------------
-// Launch wrappers that need the gather kernel's shape.
-// ------------------------------------------------------------------------------------------------
-namespace rtd {
-cudaError_t launch_gather(const GatherParams &p, cudaStream_t st) {
-    dim3 block(8, 8);
-    dim3 grid((p.ip.width + 7) / 8, (p.ip.height + 7) / 8);
-    gather_kernel<<<grid, block, 0, st>>>(p);
-    return cudaGetLastError();
-}
-}  // namespace rtd
