@@ -242,6 +242,70 @@ def load_traffic(workload: str) -> float | None:
     return None
 
 
+def photon_denoise_stages(steps: int, warmup: int, peak: float) -> dict:
+    """Config 3's pipeline on the 555-unit Cornell box at 1920x1080: 1,048,576 photons traced from the
+    ceiling light (depth 6), binned into the 128^3 grid (cell = extent / 128, radius = cell / 2), then
+    progressive frames at 4 spp with the photon lookup and the two a-trous passes.  Device times come
+    from the renderer's CUDA events."""
+    import rustracer_gb300 as rt
+
+    scene = rt.Scene.cornell555()
+    cfg = rt.RenderConfig(width=1920, height=1080, spp=4, accumulate_frames=64, enable_denoise=True,
+                          enable_photon_map=True, photon_count=1 << 20, grid_max_dim=130, photon_radius_mode=1,
+                          photon_scale=2000.0)
+    r = rt.Renderer(scene, cfg)
+    r.update_camera(scene.default_camera())
+    r.rebuild_photons()  # warm-up
+    trace_ms, grid_ms = [], []
+    for _ in range(max(steps // 4, 2)):
+        r.rebuild_photons()
+        st = r.stats()
+        trace_ms.append(st.ms_photon_trace)
+        grid_ms.append(st.ms_grid_build)
+    binned = r.stats().photons_stored
+    gp = r.grid_params()
+    slots, cells = gp.photon_slots, gp.num_cells
+    for _ in range(warmup):
+        r.record_frame()
+    r.stats()
+    for _ in range(steps):
+        r.record_frame()
+    st = r.stats()
+    frames = max(st.timed_frames, 1)
+    den_ms = st.ms_denoise_sum / frames
+    res_ms = st.ms_resolve_sum / frames
+    gat_ms = st.ms_gather_sum / frames
+    npix = cfg.width * cfg.height
+    t_ms, g_ms = statistics.median(trace_ms), statistics.median(grid_ms)
+    # Compulsory bytes of this dataflow (the trace emits u32 keys): keys read by count and scatter
+    # (4 + 4 B/slot), (start, count) written and counts read twice by the scan (16 B/cell), slot
+    # order written by scatter and read/written by the per-cell order pass (4 + 8 B per binned
+    # photon), and the 64 B photon read + 64 B write of the final gather.
+    grid_bytes = 8.0 * slots + 16.0 * cells + (12.0 + 128.0 + 4.0) * binned
+    den_bytes = 2 * 64.0 * npix
+    res_bytes = 52.0 * npix
+    r.close()
+    return {
+        "workload": "cornell555 1920x1080, 2^20 photons, 128^3 grid, spp 4, denoise 2 passes",
+        "photons_per_s": (1 << 20) / (t_ms / 1000.0),
+        "photon_trace_ms": t_ms,
+        "grid_keys_per_s": slots / (g_ms / 1000.0),
+        "grid_build_ms": g_ms, "photon_slots": slots, "binned_photons": int(binned), "cells": cells,
+        "grid_roofline": {"bound": "hbm", "achieved": grid_bytes / (g_ms / 1000.0) / 1e9, "peak": peak,
+                          "unit": "GB/s", "frac": grid_bytes / (g_ms / 1000.0) / 1e9 / peak,
+                          "algorithmic_bytes": grid_bytes},
+        "denoised_mpix_per_s": npix / (den_ms / 1000.0) / 1e6,
+        "denoise_ms_2pass": den_ms,
+        "denoise_roofline": {"bound": "hbm", "achieved": den_bytes / (den_ms / 1000.0) / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": den_bytes / (den_ms / 1000.0) / 1e9 / peak,
+                             "algorithmic_bytes": den_bytes},
+        "resolve_ms": res_ms,
+        "resolve_roofline": {"achieved": res_bytes / (res_ms / 1000.0) / 1e9, "frac":
+                             res_bytes / (res_ms / 1000.0) / 1e9 / peak},
+        "gather_ms_with_photons": gat_ms,
+    }
+
+
 def run_ours(args, w):
     import torch
 
@@ -345,6 +409,7 @@ def run_ours(args, w):
         peak, peak_kind = hbm_peak()
         achieved = algo / (gather_ms / 1000.0) / 1e9
         traffic = load_traffic(args.workload)
+        stages = photon_denoise_stages(args.steps, args.warmup, peak) if args.stages else None
         line = {
             "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -365,6 +430,7 @@ def run_ours(args, w):
             "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": 96 + 80,
                     "d2h_bytes_per_step": int(cfg.width * cfg.height * 4)},
             "clocks": clocks,
+            "stages": stages,
         }
         print(json.dumps(line), flush=True)
     r.close()
@@ -381,6 +447,8 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="icosphere1080p")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="size of the CPU-baseline sample")
+    ap.add_argument("--no-stages", dest="stages", action="store_false",
+                    help="skip the photon-map / denoise stage measurements")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]

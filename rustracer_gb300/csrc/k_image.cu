@@ -69,11 +69,107 @@ __global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__
     out[idx] = make_float4(o.x, o.y, o.z, 1.0f);
 }
 
+// The same pass for steps 1 and 2 (the reference's two passes) over a 32 x 8 pixel tile staged in
+// shared memory with a 2*step halo: colour with its luminance, normal with depth, and the raw
+// per-pixel variance of the moments with a 1-pixel halo.  Weights are evaluated as
+// sw * pow(n.n', phi_n) * exp(-(|dc - dn| / (phi_d max(dc, 1e-4)) + dl^2 / (lambda var + 1e-6))),
+// the reference's product with the two exponentials merged and pow(x, 12) taken by squaring; this
+// file is compiled with FMA contraction.  Results differ from the separate expf / powf form by a few
+// ulps of the weights.
+template <int kStep>
+__global__ void __launch_bounds__(256) denoise_tiled_kernel(const float4 *__restrict__ in, float4 *__restrict__ out,
+                                                            const float4 *__restrict__ gbuffer,
+                                                            const float4 *__restrict__ moments,
+                                                            const rt_denoise_params p) {
+    constexpr int BX = 32, BY = 8, H = 2 * kStep, TW = BX + 2 * H, TH = BY + 2 * H;
+    __shared__ float4 s_cl[TH][TW];
+    __shared__ float4 s_nd[TH][TW];
+    __shared__ float s_var[BY + 2][BX + 2];
+    const int W = (int)p.width, Hh = (int)p.height;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    const int x0 = (int)blockIdx.x * BX, y0 = (int)blockIdx.y * BY;
+    for (int i = tid; i < TW * TH; i += BX * BY) {
+        const int ty = i / TW, tx = i - ty * TW;
+        const int gx = x0 - H + tx, gy = y0 - H + ty;
+        if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
+            const size_t g = (size_t)gy * W + gx;
+            const float4 c = __ldg(in + g);
+            s_cl[ty][tx] = make_float4(c.x, c.y, c.z, luminance(mk3(c.x, c.y, c.z)));
+            s_nd[ty][tx] = __ldg(gbuffer + g);
+        }
+    }
+    for (int i = tid; i < (BX + 2) * (BY + 2); i += BX * BY) {
+        const int ty = i / (BX + 2), tx = i - ty * (BX + 2);
+        const int gx = x0 - 1 + tx, gy = y0 - 1 + ty;
+        float v = -1.0f;  // outside the image
+        if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
+            const float2 m = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
+            v = fmaxf(m.y - m.x * m.x, 0.0f);
+        }
+        s_var[ty][tx] = v;
+    }
+    __syncthreads();
+    const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+    if (x >= W || y >= Hh) return;
+    const int lx = (int)threadIdx.x + H, ly = (int)threadIdx.y + H;
+    const float4 cc = s_cl[ly][lx];
+    const float4 cn = s_nd[ly][lx];
+    float var_acc = 0.0f, var_cnt = 0.0f;
+#pragma unroll
+    for (int qy = 0; qy < 3; ++qy)
+#pragma unroll
+        for (int qx = 0; qx < 3; ++qx) {
+            const float v = s_var[threadIdx.y + qy][threadIdx.x + qx];
+            if (v >= 0.0f) {
+                var_acc += v;
+                var_cnt += 1.0f;
+            }
+        }
+    const float var_frame = var_acc / fmaxf(var_cnt, 1.0f);
+    const float ema_scale = p.alpha / fmaxf(2.0f - p.alpha, 1e-4f);
+    const float var_c = var_frame * ema_scale;
+    const float inv_dc = 1.0f / (var_c * p.lambda + 1e-6f);
+    const float inv_dd = 1.0f / (p.phi_depth * fmaxf(cn.w, 1e-4f));
+    const bool pow12 = p.phi_normal == 12.0f;
+    const float k1d[3] = {0.375f, 0.25f, 0.0625f};
+    float sr = 0.0f, sg = 0.0f, sb = 0.0f, total = 0.0f;
+#pragma unroll
+    for (int dy = -2; dy <= 2; ++dy) {
+#pragma unroll
+        for (int dx = -2; dx <= 2; ++dx) {
+            const int nx = x + dx * kStep, ny = y + dy * kStep;
+            if (nx < 0 || ny < 0 || nx >= W || ny >= Hh) continue;
+            const float4 nb = s_cl[ly + dy * kStep][lx + dx * kStep];
+            const float4 nd = s_nd[ly + dy * kStep][lx + dx * kStep];
+            const float d = fmaxf(cn.x * nd.x + cn.y * nd.y + cn.z * nd.z, 0.0f);
+            float nw;
+            if (pow12) {
+                const float d2 = d * d, d4 = d2 * d2, d8 = d4 * d4;
+                nw = d8 * d4;
+            } else {
+                nw = powf(d, p.phi_normal);
+            }
+            const float dl = nb.w - cc.w;
+            const float e = __expf(-(fabsf(cn.w - nd.w) * inv_dd + dl * dl * inv_dc));
+            const float w = (k1d[dx < 0 ? -dx : dx] * k1d[dy < 0 ? -dy : dy]) * nw * e;
+            sr += nb.x * w;
+            sg += nb.y * w;
+            sb += nb.z * w;
+            total += w;
+        }
+    }
+    const size_t idx = (size_t)y * W + x;
+    if (total > 1e-6f) out[idx] = make_float4(sr / total, sg / total, sb / total, 1.0f);
+    else out[idx] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+}
+
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
                            const rt_denoise_params &p, cudaStream_t st) {
     dim3 block(32, 8);
     dim3 grid((p.width + block.x - 1) / block.x, (p.height + block.y - 1) / block.y);
-    denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    if (p.step_size == 1u) denoise_tiled_kernel<1><<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    else if (p.step_size == 2u) denoise_tiled_kernel<2><<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    else denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
     return cudaGetLastError();
 }
 
