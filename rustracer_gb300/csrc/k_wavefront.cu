@@ -246,19 +246,80 @@ __global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant_
 }
 
 // ------------------------------------------------------------------------------------------------
-// extend: closest hit of each queued path.
+// Persistent traversal warps.  A warp takes chunks of kChunk work items with one atomic and hands them
+// to its idle lanes; every lane then advances its traversal by up to kSteps records before the warp
+// refills again, so lanes whose ray finished early pick up new rays instead of idling.
 // ------------------------------------------------------------------------------------------------
+constexpr uint32_t kChunk = 64;
+constexpr int kSteps = 8;
+
+struct WarpFeed {
+    uint32_t next = 0, end = 0;
+    bool more = true;
+};
+
+// Gives each lane with need == true the next item index (or none when the items ran out).  Every lane
+// of the warp calls it; returns the lane's index or 0xFFFFFFFF.
+__device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n, uint32_t *fetch) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t mine = 0xFFFFFFFFu;
+    uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
+    while (mask != 0u && f.more) {
+        if (f.next >= f.end) {
+            uint32_t base = 0;
+            if (lane == 0u) base = atomicAdd(fetch, kChunk);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) {
+                f.more = false;
+                break;
+            }
+            f.next = base;
+            f.end = min(base + kChunk, n);
+        }
+        const uint32_t avail = f.end - f.next;
+        const uint32_t rank = __popc(mask & lanemask_lt());
+        if (need && rank < avail) {
+            mine = f.next + rank;
+            need = false;
+        }
+        f.next += min((uint32_t)__popc(mask), avail);
+        mask = __ballot_sync(0xFFFFFFFFu, need);
+    }
+    return mine;
+}
+
+// extend: closest hit of each queued path.
 template <int kStack>
 __global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
     __shared__ uint32_t stack_smem[kStack * 128];
     uint32_t *stk = stack_smem + threadIdx.x;
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t pix = q[i];
-        const float4 o = p.ro[pix], d = p.rd[pix];
-        Hit h = trace<false>(p.scene, xyz(o), xyz(d), kInf, stk, 128u);
-        p.hit[pix] = make_float2(h.t, __uint_as_float(h.prim));
+    uint32_t *fetch = p.counts + 4 * iter + 2;
+    const DevScene &s = p.scene;
+    WarpFeed feed;
+    TravState st;
+    bool has = false;
+    uint32_t pix = 0;
+    for (;;) {
+        const uint32_t item = warp_take(feed, !has, n, fetch);
+        if (item != 0xFFFFFFFFu) {
+            pix = q[item];
+            const float4 o = p.ro[pix], d = p.rd[pix];
+            st = trav_begin(xyz(o), xyz(d), kInf);
+            has = true;
+            if (s.cnode_count == 0u) {
+                p.hit[pix] = make_float2(kInf, 0.0f);
+                has = false;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, has)) break;
+        for (int k = 0; k < kSteps && has; ++k) {
+            if (trav_step<false>(s, st, stk, 128u)) {
+                p.hit[pix] = make_float2(st.t, __uint_as_float(st.prim));
+                has = false;
+            }
+        }
     }
 }
 
@@ -566,40 +627,61 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
 // ------------------------------------------------------------------------------------------------
 // shadow: the deferred NEE occlusion test (gather.wgsl:91-103) and the contribution of visible lights.
 // ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec_i, const TravState &st, float limit) {
+    const DevScene &s = p.scene;
+    const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1], c = p.shadow[3ull * rec_i + 2];
+    bool shadowed = !(st.t >= limit);
+    if (shadowed && !s.any_hit_shadows) {
+        TriFull bt = load_tri(s, st.prim);
+        Mat bm = load_mat(s, bt.material_id);
+        if ((bm.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && bm.tex_albedo != RT_TEX_NONE) {
+            Bary b = barycentric(bt, xyz(o), xyz(d), st.t);
+            if (tex_sample(s.tex[RT_TEX_ALBEDO], b.uvx, b.uvy, (int32_t)bm.tex_albedo).w < 0.5f) shadowed = false;
+        }
+    }
+    if (shadowed) return;
+    const uint32_t pix = __float_as_uint(d.w);
+    const uint32_t tag = __float_as_uint(c.w);
+    Accum A = load_acc(p, pix);
+    const float4 acc1 = p.acc[4 * (size_t)pix + 1];
+    if (tag & 0x10000u) add_luma(tag & 0xFFFFu, A, xyz(c));
+    else add_radiance(tag & 0xFFFFu, A, xyz(c));
+    store_acc(p, pix, A, acc1);
+}
+
 template <int kStack>
 __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
     __shared__ uint32_t stack_smem[kStack * 128];
     uint32_t *stk = stack_smem + threadIdx.x;
     const uint32_t m = p.counts[4 * iter + 1];
+    uint32_t *fetch = p.counts + 4 * iter + 3;
     const DevScene &s = p.scene;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const float4 *rec = p.shadow + 3ull * i;
-        const float4 o = rec[0], d = rec[1], c = rec[2];
-        const f3 origin = xyz(o), dir = xyz(d);
-        const float limit = o.w - 0.001f;
-        bool shadowed;
-        if (s.any_hit_shadows) {
-            shadowed = trace<true>(s, origin, dir, limit, stk, 128u).t < kInf;
-        } else {
-            Hit sh = trace<false>(s, origin, dir, kInf, stk, 128u);
-            shadowed = !(sh.t >= limit);
-            if (shadowed) {
-                TriFull bt = load_tri(s, sh.prim);
-                Mat bm = load_mat(s, bt.material_id);
-                if ((bm.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && bm.tex_albedo != RT_TEX_NONE) {
-                    Bary b = barycentric(bt, origin, dir, sh.t);
-                    if (tex_sample(s.tex[RT_TEX_ALBEDO], b.uvx, b.uvy, (int32_t)bm.tex_albedo).w < 0.5f) shadowed = false;
-                }
+    WarpFeed feed;
+    TravState st;
+    bool has = false;
+    uint32_t rec_i = 0;
+    float limit = 0.0f;
+    for (;;) {
+        const uint32_t item = warp_take(feed, !has, m, fetch);
+        if (item != 0xFFFFFFFFu) {
+            rec_i = item;
+            const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1];
+            limit = o.w - 0.001f;
+            // Without cut-out materials the occlusion test may stop at the first triangle below the
+            // limit; with them the reference's closest-hit-then-alpha rule is kept.
+            st = trav_begin(xyz(o), xyz(d), s.any_hit_shadows ? limit : kInf);
+            has = s.cnode_count != 0u;
+            if (!has) st.t = kInf;
+            if (!has) shadow_resolve(p, rec_i, st, limit);
+        }
+        if (!__any_sync(0xFFFFFFFFu, has)) break;
+        for (int k = 0; k < kSteps && has; ++k) {
+            const bool done = s.any_hit_shadows ? trav_step<true>(s, st, stk, 128u) : trav_step<false>(s, st, stk, 128u);
+            if (done) {
+                shadow_resolve(p, rec_i, st, limit);
+                has = false;
             }
         }
-        if (shadowed) continue;
-        const uint32_t pix = __float_as_uint(d.w);
-        const uint32_t tag = __float_as_uint(c.w);
-        Accum A = load_acc(p, pix);
-        const float4 acc1 = p.acc[4 * (size_t)pix + 1];
-        if (tag & 0x10000u) add_luma(tag & 0xFFFFu, A, xyz(c));
-        else add_radiance(tag & 0xFFFFu, A, xyz(c));
-        store_acc(p, pix, A, acc1);
     }
 }
 

@@ -260,89 +260,116 @@ struct Hit {
 // BVH traversal over the child-pair records.  Each record fetch tests both children's boxes with the
 // reference's slab test (gather.wgsl:71-75: (bmin - ro) / d, te <= ta && ta > 0 && te < t); leaf
 // children are intersected on the spot, internal children are visited nearest entry first with the
-// farther one pushed (a push is dropped once `cap` entries are in use, as the reference drops pushes
-// at 63).  The tree is the reference's, so the closest hit is the reference's: only triangles with
-// exactly equal t may resolve to a different one of them.  The stack lives in shared memory, one
+// farther one pushed (a push is dropped once `stack_cap` entries are in use, as the reference drops
+// pushes at 63).  The tree is the reference's, so the closest hit is the reference's: only triangles
+// with exactly equal t may resolve to a different one of them.  The stack lives in shared memory, one
 // 4-byte column per thread.
 //
 // kAny: stop at the first triangle with t < t_limit (occlusion query); otherwise the closest hit below
-// t_limit.
+// t_limit.  TravState / trav_step make the traversal resumable one record at a time, so persistent
+// warps can refill lanes whose ray finished.
+struct TravState {
+    f3 ro, rd, inv;
+    float t;
+    uint32_t prim, node, sp;
+};
+
+__device__ __forceinline__ TravState trav_begin(f3 ro, f3 rd, float t_limit) {
+    TravState st;
+    st.ro = ro;
+    st.rd = rd;
+    st.inv = mk3(1.0f, 1.0f, 1.0f) / rd;
+    st.t = t_limit;
+    st.prim = 0u;
+    st.node = 0u;
+    st.sp = 0u;
+    return st;
+}
+
+// Visits one record.  Returns true when the traversal has finished (st.t / st.prim hold the result;
+// for kAny, st.t < the limit means an occluder was found).
+template <bool kAny>
+__device__ __forceinline__ bool trav_step(const DevScene &s, TravState &st, uint32_t *stk, uint32_t stride) {
+    const float4 *np = s.cnodes + 4ull * st.node;
+    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+    const f3 ro = st.ro, rd = st.rd, inv = st.inv;
+    const f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
+    const f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
+    const float le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
+    const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
+    const float re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
+    const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
+    bool hl = le <= lx && lx > 0.0f && le < st.t;
+    bool hr = re <= rx && rx > 0.0f && re < st.t;
+    const uint32_t lref = __float_as_uint(q0.w), lcnt = __float_as_uint(q1.w);
+    const uint32_t rref = __float_as_uint(q2.w), rcnt = __float_as_uint(q3.w);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const bool h = side == 0 ? hl : hr;
+        const uint32_t cnt = side == 0 ? lcnt : rcnt;
+        if (h && cnt) {
+            const uint32_t first = side == 0 ? lref : rref;
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const float4 *tp = s.tri_ord + 3ull * (first + k);
+                const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+                // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
+                const f3 h3 = cross(rd, xyz(e2));
+                const float a = dot(xyz(e1), h3);
+                float t = kInf;
+                if (!(fabsf(a) < 1e-7f)) {
+                    const float f = 1.0f / a;
+                    const f3 sv = ro - xyz(v0);
+                    const float u = f * dot(sv, h3);
+                    if (!(u < 0.0f || u > 1.0f)) {
+                        const f3 q = cross(sv, xyz(e1));
+                        const float v = f * dot(rd, q);
+                        if (!(v < 0.0f || u + v > 1.0f)) {
+                            const float tt = f * dot(xyz(e2), q);
+                            if (tt > kEps) t = tt;
+                        }
+                    }
+                }
+                if (t < st.t) {
+                    st.t = t;
+                    st.prim = __float_as_uint(v0.w);
+                    if (kAny) return true;
+                }
+            }
+            if (side == 0) hl = false;
+            else hr = false;
+        }
+    }
+    if (hl && hr) {
+        const bool left_first = le <= re;
+        const uint32_t far = left_first ? rref : lref;
+        st.node = left_first ? lref : rref;
+        if (st.sp < s.stack_cap) {
+            stk[st.sp * stride] = far;
+            st.sp += 1u;
+        }
+    } else if (hl) {
+        st.node = lref;
+    } else if (hr) {
+        st.node = rref;
+    } else {
+        if (st.sp == 0u) return true;
+        st.sp -= 1u;
+        st.node = stk[st.sp * stride];
+    }
+    return false;
+}
+
 template <bool kAny>
 __device__ __forceinline__ Hit trace(const DevScene &s, f3 ro, f3 rd, float t_limit, uint32_t *stk,
                                      uint32_t stride) {
-    Hit hit{t_limit, 0u};
     if (s.cnode_count == 0u) return Hit{kInf, 0u};
-    const f3 inv = mk3(1.0f, 1.0f, 1.0f) / rd;
-    const uint32_t cap = s.stack_cap;
-    uint32_t node = 0u, sp = 0u;
-    for (;;) {
-        const float4 *np = s.cnodes + 4ull * node;
-        const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-        f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
-        f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
-        const float le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
-        const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
-        const float re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
-        const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
-        bool hl = le <= lx && lx > 0.0f && le < hit.t;
-        bool hr = re <= rx && rx > 0.0f && re < hit.t;
-        const uint32_t lref = __float_as_uint(q0.w), lcnt = __float_as_uint(q1.w);
-        const uint32_t rref = __float_as_uint(q2.w), rcnt = __float_as_uint(q3.w);
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const bool h = side == 0 ? hl : hr;
-            const uint32_t cnt = side == 0 ? lcnt : rcnt;
-            if (h && cnt) {
-                const uint32_t first = side == 0 ? lref : rref;
-                for (uint32_t k = 0; k < cnt; ++k) {
-                    const float4 *tp = s.tri_ord + 3ull * (first + k);
-                    const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
-                    const f3 h3 = cross(rd, xyz(e2));
-                    const float a = dot(xyz(e1), h3);
-                    float t = kInf;
-                    if (!(fabsf(a) < 1e-7f)) {
-                        const float f = 1.0f / a;
-                        const f3 sv = ro - xyz(v0);
-                        const float u = f * dot(sv, h3);
-                        if (!(u < 0.0f || u > 1.0f)) {
-                            const f3 q = cross(sv, xyz(e1));
-                            const float v = f * dot(rd, q);
-                            if (!(v < 0.0f || u + v > 1.0f)) {
-                                const float tt = f * dot(xyz(e2), q);
-                                if (tt > kEps) t = tt;
-                            }
-                        }
-                    }
-                    if (t < hit.t) {
-                        hit.t = t;
-                        hit.prim = __float_as_uint(v0.w);
-                        if (kAny) return hit;
-                    }
-                }
-                if (side == 0) hl = false;
-                else hr = false;
-            }
-        }
-        if (hl && hr) {
-            const bool left_first = le <= re;
-            const uint32_t far = left_first ? rref : lref;
-            node = left_first ? lref : rref;
-            if (sp < cap) {
-                stk[sp * stride] = far;
-                sp += 1u;
-            }
-        } else if (hl) {
-            node = lref;
-        } else if (hr) {
-            node = rref;
-        } else {
-            if (sp == 0u) break;
-            sp -= 1u;
-            node = stk[sp * stride];
-        }
+    TravState st = trav_begin(ro, rd, t_limit);
+    bool found = false;
+    while (!trav_step<kAny>(s, st, stk, stride)) {
     }
-    if (kAny) hit.t = kInf;  // nothing closer than the limit
-    return hit;
+    if (kAny) found = st.t < t_limit;
+    if (kAny) return Hit{found ? st.t : kInf, st.prim};
+    return Hit{st.t, st.prim};
 }
 
 struct Bary {
