@@ -182,9 +182,11 @@ __global__ void __launch_bounds__(256) resolve_kernel(const float4 *__restrict__
     if (i >= npix) return;
     const float4 f = __ldg(frame + i);
     const float4 a = accum[i];
+    // mix(prev, fresh, alpha) rounded as two products and a sum (no contraction: this file is
+    // compiled with FMA, the composite stays bit-exact).
     const float om = 1.0f - alpha;
-    const float4 h = make_float4(a.x * om + f.x * alpha, a.y * om + f.y * alpha, a.z * om + f.z * alpha,
-                                 a.w * om + f.w * alpha);
+    auto mixr = [&](float x, float y) { return __fadd_rn(__fmul_rn(x, om), __fmul_rn(y, alpha)); };
+    const float4 h = make_float4(mixr(a.x, f.x), mixr(a.y, f.y), mixr(a.z, f.z), mixr(a.w, f.w));
     accum[i] = h;
     const f3 exposed = mk3(h.x, h.y, h.z) * tp.exposure;
     const f3 mapped = exposed / (exposed + mk3(1.0f, 1.0f, 1.0f));
