@@ -345,6 +345,27 @@ int rt_stage_resolve(const float *frame_rgba, float *accum_inout, const float *g
 int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_params *gp, uint32_t *counts, uint32_t *meta,
                          rt_photon *sorted);
 
+/* The photon-grid build of rt_stage_photon_grid without any device allocation.  It has no
+ * counterpart in the reference.  It exists for callers that cannot allocate device memory: frame loops
+ * with a no-allocation rule (cudaMalloc / cudaFree can synchronise the device), hosts whose device
+ * memory all comes from their own allocator or pool, and processes near the memory limit.
+ *   - d_photons (gp->photon_slots records), d_counts (gp->num_cells), d_meta (2 * gp->num_cells) and
+ *     d_sorted (gp->photon_slots records) are DEVICE pointers owned by the caller; entries of d_sorted
+ *     past the number of binned photons are left as they were.
+ *   - Scratch lives in one file-scope device array of RT_NOALLOC_SCRATCH_BYTES that every GPU loading
+ *     the library holds until the process exits; sizes above RT_NOALLOC_MAX_SLOTS slots or
+ *     RT_NOALLOC_MAX_CELLS cells are rejected with RT_ERR_INVALID_ARGUMENT.
+ *   - The first call on a device looks up that array's device address with the device current; make
+ *     that first call before any stream capture.
+ *   - Work is enqueued on `stream` (a cudaStream_t; NULL = the default stream) and the call returns
+ *     without waiting.  All calls share the one array (its counters are cleared by each call): calls
+ *     whose work overlaps on the GPU race, so order them on one stream or synchronise between them. */
+#define RT_NOALLOC_MAX_SLOTS (1u << 20)
+#define RT_NOALLOC_MAX_CELLS (1u << 18)
+#define RT_NOALLOC_SCRATCH_BYTES 9438208u
+int rt_stage_photon_grid_noalloc(const rt_photon *d_photons, const rt_grid_params *gp, uint32_t *d_counts,
+                                 uint32_t *d_meta, rt_photon *d_sorted, void *stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Host-side scene model (rustracer-core): meshes, materials, lights, role textures, flattening and
  * the binned-SAH BVH build.  Used by the headless entry, the tests and the benchmarks; a Rust

@@ -30,6 +30,9 @@ GRID_MAX_DIM = 26
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE = 0, 1, 2, 3
 LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_AREA, LIGHT_ENVIRONMENT = 0, 1, 2, 3
 TEX_ALBEDO, TEX_MR, TEX_EMISSIVE, TEX_NORMAL = 0, 1, 2, 3
+NOALLOC_MAX_SLOTS = 1 << 20
+NOALLOC_MAX_CELLS = 1 << 18
+NOALLOC_SCRATCH_BYTES = 9438208
 
 f3 = C.c_float * 3
 f4 = C.c_float * 4
@@ -176,6 +179,7 @@ _PROTOS: dict[str, tuple] = {
     "rt_stage_denoise": (C.c_int, [vp, vp, vp, u32, u32, C.c_float, u32, vp]),
     "rt_stage_resolve": (C.c_int, [vp, vp, vp, u32, u32, C.c_float, P(TonemapParams), vp]),
     "rt_stage_photon_grid": (C.c_int, [vp, P(GridParams), vp, vp, vp]),
+    "rt_stage_photon_grid_noalloc": (C.c_int, [vp, P(GridParams), vp, vp, vp, vp]),
     "rt_scene_create": (C.c_int, [P(vp)]),
     "rt_scene_destroy": (None, [vp]),
     "rt_scene_add_mesh": (C.c_int, [vp, vp, vp, vp, C.c_uint64, vp, C.c_uint64, u32]),
