@@ -69,28 +69,101 @@ __global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__
     out[idx] = make_float4(o.x, o.y, o.z, 1.0f);
 }
 
-// The same pass for steps 1 and 2 (the reference's two passes) over a 32 x 8 pixel tile staged in
+// The same pass for steps 1 and 2 (the reference's two passes) over a 32 x 32 pixel tile staged in
 // shared memory with a 2*step halo: colour with its luminance, normal with depth, and the raw
-// per-pixel variance of the moments with a 1-pixel halo.  Weights are evaluated as
-// sw * pow(n.n', phi_n) * exp(-(|dc - dn| / (phi_d max(dc, 1e-4)) + dl^2 / (lambda var + 1e-6))),
+// per-pixel variance of the moments with a 1-pixel halo.  Each thread computes four pixels of one
+// column, (x, y + k*step) for k = 0..3, whose 5 x 5 tap windows share four of their five rows, so a
+// tap row is read from shared memory once for up to four pixels (40 reads for 4 pixels instead of
+// 100); a warp's lanes read consecutive x (no bank conflicts).  Tiles entirely inside the image skip
+// the bounds tests.  Weights are evaluated as
+//   sw * pow(n.n', phi_n) * exp(-(|dc - dn| / (phi_d max(dc, 1e-4)) + dl^2 / (lambda var + 1e-6))),
 // the reference's product with the two exponentials merged and pow(x, 12) taken by squaring; this
 // file is compiled with FMA contraction.  Results differ from the separate expf / powf form by a few
 // ulps of the weights.
+constexpr int kDnBX = 32, kDnRows = 32, kDnThreadsY = 8, kDnPix = 4;
+
+template <int kStep, bool kInterior>
+__device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * kStep],
+                                               const float4 (*s_nd)[kDnBX + 4 * kStep], const float *s_varc,
+                                               int lx, int ly0, int x, int y0, int W, int Hh, const rt_denoise_params &p,
+                                               float4 *__restrict__ out) {
+    constexpr int H = 2 * kStep;
+    const float k1d[3] = {0.375f, 0.25f, 0.0625f};
+    const bool pow12 = p.phi_normal == 12.0f;
+    float4 cc[kDnPix], cn[kDnPix];
+    float inv_dc[kDnPix], inv_dd[kDnPix];
+    float sr[kDnPix], sg[kDnPix], sb[kDnPix], tot[kDnPix];
+#pragma unroll
+    for (int k = 0; k < kDnPix; ++k) {
+        cc[k] = s_cl[ly0 + H + k * kStep][lx + H];
+        cn[k] = s_nd[ly0 + H + k * kStep][lx + H];
+        inv_dc[k] = 1.0f / (s_varc[k] * p.lambda + 1e-6f);
+        inv_dd[k] = 1.0f / (p.phi_depth * fmaxf(cn[k].w, 1e-4f));
+        sr[k] = sg[k] = sb[k] = tot[k] = 0.0f;
+    }
+    // Tap rows j = 0 .. 7 (row offset (j - 2) * step from the first pixel); pixel k uses rows k .. k+4.
+#pragma unroll
+    for (int j = 0; j < kDnPix + 4; ++j) {
+        const int ty = ly0 + j * kStep;  // tile row of this tap row
+#pragma unroll
+        for (int dx = -2; dx <= 2; ++dx) {
+            const int nx = x + dx * kStep;
+            if (!kInterior && (nx < 0 || nx >= W)) continue;
+            const float4 nb = s_cl[ty][lx + H + dx * kStep];
+            const float4 nd = s_nd[ty][lx + H + dx * kStep];
+#pragma unroll
+            for (int k = 0; k < kDnPix; ++k) {
+                const int dy = j - k - 2;
+                if (dy < -2 || dy > 2) continue;
+                if (!kInterior) {
+                    const int ny = y0 + (j - 2) * kStep;
+                    if (ny < 0 || ny >= Hh || y0 + k * kStep >= Hh) continue;
+                }
+                const float d = fmaxf(cn[k].x * nd.x + cn[k].y * nd.y + cn[k].z * nd.z, 0.0f);
+                float nw;
+                if (pow12) {
+                    const float d2 = d * d, d4 = d2 * d2, d8 = d4 * d4;
+                    nw = d8 * d4;
+                } else {
+                    nw = powf(d, p.phi_normal);
+                }
+                const float dl = nb.w - cc[k].w;
+                const float e = __expf(-(fabsf(cn[k].w - nd.w) * inv_dd[k] + dl * dl * inv_dc[k]));
+                const float w = (k1d[dx < 0 ? -dx : dx] * k1d[dy < 0 ? -dy : dy]) * nw * e;
+                sr[k] += nb.x * w;
+                sg[k] += nb.y * w;
+                sb[k] += nb.z * w;
+                tot[k] += w;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kDnPix; ++k) {
+        const int y = y0 + k * kStep;
+        if (!kInterior && (x >= W || y >= Hh)) continue;
+        const size_t idx = (size_t)y * W + x;
+        if (tot[k] > 1e-6f) out[idx] = make_float4(sr[k] / tot[k], sg[k] / tot[k], sb[k] / tot[k], 1.0f);
+        else out[idx] = make_float4(cc[k].x, cc[k].y, cc[k].z, 1.0f);
+    }
+}
+
 template <int kStep>
-__global__ void __launch_bounds__(256) denoise_tiled_kernel(const float4 *__restrict__ in, float4 *__restrict__ out,
-                                                            const float4 *__restrict__ gbuffer,
-                                                            const float4 *__restrict__ moments,
-                                                            const rt_denoise_params p) {
-    constexpr int BX = 32, BY = 8, H = 2 * kStep, TW = BX + 2 * H, TH = BY + 2 * H;
-    __shared__ float4 s_cl[TH][TW];
-    __shared__ float4 s_nd[TH][TW];
-    __shared__ float s_var[BY + 2][BX + 2];
+__global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(const float4 *__restrict__ in,
+                                                                           float4 *__restrict__ out,
+                                                                           const float4 *__restrict__ gbuffer,
+                                                                           const float4 *__restrict__ moments,
+                                                                           const rt_denoise_params p) {
+    constexpr int H = 2 * kStep, TW = kDnBX + 2 * H, TH = kDnRows + 2 * H;
+    extern __shared__ float4 dn_smem[];
+    float4(*s_cl)[TW] = reinterpret_cast<float4(*)[TW]>(dn_smem);
+    float4(*s_nd)[TW] = reinterpret_cast<float4(*)[TW]>(dn_smem + TW * TH);
+    float(*s_var)[kDnBX + 2] = reinterpret_cast<float(*)[kDnBX + 2]>(dn_smem + 2 * TW * TH);
     const int W = (int)p.width, Hh = (int)p.height;
-    const int tid = threadIdx.y * BX + threadIdx.x;
-    const int x0 = (int)blockIdx.x * BX, y0 = (int)blockIdx.y * BY;
-    for (int i = tid; i < TW * TH; i += BX * BY) {
+    const int tid = threadIdx.y * kDnBX + threadIdx.x;
+    const int x0 = (int)blockIdx.x * kDnBX, y0t = (int)blockIdx.y * kDnRows;
+    for (int i = tid; i < TW * TH; i += kDnBX * kDnThreadsY) {
         const int ty = i / TW, tx = i - ty * TW;
-        const int gx = x0 - H + tx, gy = y0 - H + ty;
+        const int gx = x0 - H + tx, gy = y0t - H + ty;
         if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
             const size_t g = (size_t)gy * W + gx;
             const float4 c = __ldg(in + g);
@@ -98,9 +171,9 @@ __global__ void __launch_bounds__(256) denoise_tiled_kernel(const float4 *__rest
             s_nd[ty][tx] = __ldg(gbuffer + g);
         }
     }
-    for (int i = tid; i < (BX + 2) * (BY + 2); i += BX * BY) {
-        const int ty = i / (BX + 2), tx = i - ty * (BX + 2);
-        const int gx = x0 - 1 + tx, gy = y0 - 1 + ty;
+    for (int i = tid; i < (kDnBX + 2) * (kDnRows + 2); i += kDnBX * kDnThreadsY) {
+        const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
+        const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
         float v = -1.0f;  // outside the image
         if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
             const float2 m = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
@@ -109,67 +182,61 @@ __global__ void __launch_bounds__(256) denoise_tiled_kernel(const float4 *__rest
         s_var[ty][tx] = v;
     }
     __syncthreads();
-    const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
-    if (x >= W || y >= Hh) return;
-    const int lx = (int)threadIdx.x + H, ly = (int)threadIdx.y + H;
-    const float4 cc = s_cl[ly][lx];
-    const float4 cn = s_nd[ly][lx];
-    float var_acc = 0.0f, var_cnt = 0.0f;
-#pragma unroll
-    for (int qy = 0; qy < 3; ++qy)
-#pragma unroll
-        for (int qx = 0; qx < 3; ++qx) {
-            const float v = s_var[threadIdx.y + qy][threadIdx.x + qx];
-            if (v >= 0.0f) {
-                var_acc += v;
-                var_cnt += 1.0f;
-            }
-        }
-    const float var_frame = var_acc / fmaxf(var_cnt, 1.0f);
+    // This thread's column: rows r0 + k*step of the tile, k = 0..3.
+    const int ty = (int)threadIdx.y;
+    const int r0 = (ty / kStep) * (kDnPix * kStep) + (ty % kStep);
+    const int lx = (int)threadIdx.x, x = x0 + lx, y0 = y0t + r0;
     const float ema_scale = p.alpha / fmaxf(2.0f - p.alpha, 1e-4f);
-    const float var_c = var_frame * ema_scale;
-    const float inv_dc = 1.0f / (var_c * p.lambda + 1e-6f);
-    const float inv_dd = 1.0f / (p.phi_depth * fmaxf(cn.w, 1e-4f));
-    const bool pow12 = p.phi_normal == 12.0f;
-    const float k1d[3] = {0.375f, 0.25f, 0.0625f};
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f, total = 0.0f;
+    float varc[kDnPix];
 #pragma unroll
-    for (int dy = -2; dy <= 2; ++dy) {
+    for (int k = 0; k < kDnPix; ++k) {
+        float acc = 0.0f, cnt = 0.0f;
 #pragma unroll
-        for (int dx = -2; dx <= 2; ++dx) {
-            const int nx = x + dx * kStep, ny = y + dy * kStep;
-            if (nx < 0 || ny < 0 || nx >= W || ny >= Hh) continue;
-            const float4 nb = s_cl[ly + dy * kStep][lx + dx * kStep];
-            const float4 nd = s_nd[ly + dy * kStep][lx + dx * kStep];
-            const float d = fmaxf(cn.x * nd.x + cn.y * nd.y + cn.z * nd.z, 0.0f);
-            float nw;
-            if (pow12) {
-                const float d2 = d * d, d4 = d2 * d2, d8 = d4 * d4;
-                nw = d8 * d4;
-            } else {
-                nw = powf(d, p.phi_normal);
+        for (int qy = 0; qy < 3; ++qy)
+#pragma unroll
+            for (int qx = 0; qx < 3; ++qx) {
+                const float v = s_var[r0 + k * kStep + qy][lx + qx];
+                if (v >= 0.0f) {
+                    acc += v;
+                    cnt += 1.0f;
+                }
             }
-            const float dl = nb.w - cc.w;
-            const float e = __expf(-(fabsf(cn.w - nd.w) * inv_dd + dl * dl * inv_dc));
-            const float w = (k1d[dx < 0 ? -dx : dx] * k1d[dy < 0 ? -dy : dy]) * nw * e;
-            sr += nb.x * w;
-            sg += nb.y * w;
-            sb += nb.z * w;
-            total += w;
-        }
+        varc[k] = (acc / fmaxf(cnt, 1.0f)) * ema_scale;
     }
-    const size_t idx = (size_t)y * W + x;
-    if (total > 1e-6f) out[idx] = make_float4(sr / total, sg / total, sb / total, 1.0f);
-    else out[idx] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+    const bool interior = x0 - H >= 0 && y0t - H >= 0 && x0 + kDnBX + H <= W && y0t + kDnRows + H <= Hh;
+    if (interior)
+        denoise_column<kStep, true>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+    else
+        denoise_column<kStep, false>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+}
+
+template <int kStep>
+constexpr size_t denoise_smem_bytes() {
+    return sizeof(float4) * 2 * (kDnBX + 4 * kStep) * (kDnRows + 4 * kStep) + sizeof(float) * (kDnBX + 2) * (kDnRows + 2);
 }
 
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
                            const rt_denoise_params &p, cudaStream_t st) {
+    if (p.step_size == 1u || p.step_size == 2u) {
+        static bool attr_set = false;  // opt in to more than 48 KB of dynamic shared memory, once
+        if (!attr_set) {
+            cudaFuncSetAttribute(denoise_tiled_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)denoise_smem_bytes<1>());
+            cudaFuncSetAttribute(denoise_tiled_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)denoise_smem_bytes<2>());
+            attr_set = true;
+        }
+        dim3 block(kDnBX, kDnThreadsY);
+        dim3 grid((p.width + kDnBX - 1) / kDnBX, (p.height + kDnRows - 1) / kDnRows);
+        if (p.step_size == 1u)
+            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(in, out, gbuffer, moments, p);
+        else
+            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(in, out, gbuffer, moments, p);
+        return cudaGetLastError();
+    }
     dim3 block(32, 8);
     dim3 grid((p.width + block.x - 1) / block.x, (p.height + block.y - 1) / block.y);
-    if (p.step_size == 1u) denoise_tiled_kernel<1><<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
-    else if (p.step_size == 2u) denoise_tiled_kernel<2><<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
-    else denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
     return cudaGetLastError();
 }
 

@@ -405,12 +405,35 @@ __device__ __forceinline__ void warp_bitonic(Seg seg, uint32_t count, uint32_t l
 constexpr uint32_t kOrderWarps = 8;
 constexpr uint32_t kOrderSmem = 1024;  // per-warp shared buffer (entries)
 
-__global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
+// Cells holding two or more photons, appended to `list` (one thread per cell, coalesced meta reads).
+__global__ void __launch_bounds__(256) multi_cells_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
+                                                          uint32_t *__restrict__ list, uint32_t *__restrict__ n_list) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n_cells + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t c = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool want = c < n_cells && __ldg(&meta[c].y) > 1u;
+        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+        if (mask == 0u) continue;
+        const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(n_list, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (want) list[base + __popc(mask & lanemask_lt())] = c;
+    }
+}
+
+// One warp per listed cell: the cell's slot indices sorted ascending.
+__global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__restrict__ meta,
+                                                                  const uint32_t *__restrict__ list,
+                                                                  const uint32_t *__restrict__ n_list,
                                                                   uint32_t *__restrict__ order) {
     __shared__ uint32_t buf[kOrderWarps][kOrderSmem];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t warps_total = gridDim.x * kOrderWarps;
-    for (uint32_t c = blockIdx.x * kOrderWarps + w; c < n_cells; c += warps_total) {
+    const uint32_t n = *n_list;
+    for (uint32_t li = blockIdx.x * kOrderWarps + w; li < n; li += warps_total) {
+        const uint32_t c = __ldg(list + li);
         uint2 m = __ldg(meta + c);
         const uint32_t start = m.x, count = m.y;
         if (count <= 1u) continue;
@@ -480,7 +503,12 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (n) {
         scatter_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
-        order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(g.meta, C, g.order);
+        // The cells to order are listed in the cursor array (the cursors are spent after the scatter);
+        // the list length is total[1].
+        if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+        multi_cells_kernel<<<grid_for(C, 256, 8), 256, 0, st>>>(g.meta, C, g.cursor, g.total + 1);
+        order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(g.meta, g.cursor,
+                                                                                                g.total + 1, g.order);
         photon_gather_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

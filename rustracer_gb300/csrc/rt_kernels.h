@@ -61,7 +61,7 @@ struct GridBuffers {
     uint32_t *order;        // slot_count: slot indices in (cell, slot) order
     float4 *sorted;         // slot_count photons
     uint32_t *scan_partials;  // grid_scan_partials(num_cells) entries
-    uint32_t *total;          // 1 entry: number of binned photons
+    uint32_t *total;          // 4 entries: [0] binned photons, [1] cells holding two or more
 };
 uint32_t grid_scan_partials(uint32_t num_cells);
 cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const rt_grid_params &gp, uint32_t *keys,
