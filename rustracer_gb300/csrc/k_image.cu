@@ -161,25 +161,56 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(cons
     const int W = (int)p.width, Hh = (int)p.height;
     const int tid = threadIdx.y * kDnBX + threadIdx.x;
     const int x0 = (int)blockIdx.x * kDnBX, y0t = (int)blockIdx.y * kDnRows;
-    for (int i = tid; i < TW * TH; i += kDnBX * kDnThreadsY) {
-        const int ty = i / TW, tx = i - ty * TW;
-        const int gx = x0 - H + tx, gy = y0t - H + ty;
-        if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
-            const size_t g = (size_t)gy * W + gx;
-            const float4 c = __ldg(in + g);
-            s_cl[ty][tx] = make_float4(c.x, c.y, c.z, luminance(mk3(c.x, c.y, c.z)));
-            s_nd[ty][tx] = __ldg(gbuffer + g);
+    constexpr int kThreads = kDnBX * kDnThreadsY;
+    // Tile load: every load of this thread is issued before any shared-memory store, so a thread keeps
+    // up to 2 * kPer requests in flight instead of waiting on each in turn.
+    constexpr int kPer = (TW * TH + kThreads - 1) / kThreads;
+    {
+        float4 c[kPer], g[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = tid + k * kThreads;
+            const int ty = i / TW, tx = i - ty * TW;
+            const int gx = x0 - H + tx, gy = y0t - H + ty;
+            if (i < TW * TH && gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
+                const size_t q = (size_t)gy * W + gx;
+                c[k] = __ldg(in + q);
+                g[k] = __ldg(gbuffer + q);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = tid + k * kThreads;
+            const int ty = i / TW, tx = i - ty * TW;
+            const int gx = x0 - H + tx, gy = y0t - H + ty;
+            if (i < TW * TH && gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
+                s_cl[ty][tx] = make_float4(c[k].x, c[k].y, c[k].z, luminance(mk3(c[k].x, c[k].y, c[k].z)));
+                s_nd[ty][tx] = g[k];
+            }
         }
     }
-    for (int i = tid; i < (kDnBX + 2) * (kDnRows + 2); i += kDnBX * kDnThreadsY) {
-        const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
-        const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
-        float v = -1.0f;  // outside the image
-        if (gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
-            const float2 m = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
-            v = fmaxf(m.y - m.x * m.x, 0.0f);
+    constexpr int kVarN = (kDnBX + 2) * (kDnRows + 2);
+    constexpr int kVarPer = (kVarN + kThreads - 1) / kThreads;
+    {
+        float2 m[kVarPer];
+#pragma unroll
+        for (int k = 0; k < kVarPer; ++k) {
+            const int i = tid + k * kThreads;
+            const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
+            const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
+            m[k] = make_float2(0.0f, 0.0f);
+            if (i < kVarN && gx >= 0 && gy >= 0 && gx < W && gy < Hh)
+                m[k] = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
         }
-        s_var[ty][tx] = v;
+#pragma unroll
+        for (int k = 0; k < kVarPer; ++k) {
+            const int i = tid + k * kThreads;
+            if (i >= kVarN) continue;
+            const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
+            const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
+            // -1 marks a position outside the image
+            s_var[ty][tx] = (gx >= 0 && gy >= 0 && gx < W && gy < Hh) ? fmaxf(m[k].y - m[k].x * m[k].x, 0.0f) : -1.0f;
+        }
     }
     __syncthreads();
     // This thread's column: rows r0 + k*step of the tile, k = 0..3.

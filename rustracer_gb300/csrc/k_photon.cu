@@ -235,18 +235,32 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Four consecutive keys per thread (one 16-byte load when aligned and complete).
+__device__ __forceinline__ uint4 load_keys4(const uint32_t *__restrict__ keys, uint64_t s, uint64_t n) {
+    if (s + 3 < n) return __ldg(reinterpret_cast<const uint4 *>(keys + s));
+    uint4 k = make_uint4(kInvalidKey, kInvalidKey, kInvalidKey, kInvalidKey);
+    if (s < n) k.x = __ldg(keys + s);
+    if (s + 1 < n) k.y = __ldg(keys + s + 1);
+    if (s + 2 < n) k.z = __ldg(keys + s + 2);
+    return k;
+}
+
 // Histogram.  Lanes of a warp holding the same key are merged (match.any) into one atomic.
 __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                     uint32_t *__restrict__ counts) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
-        uint64_t s = start + r * stride;
-        uint32_t k = s < n ? __ldg(keys + s) : kInvalidKey;
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-        uint32_t leader = __ffs(peers) - 1;
-        if (k != kInvalidKey && (threadIdx.x & 31u) == leader) atomicAdd(counts + k, (uint32_t)__popc(peers));
+        const uint4 k4 = load_keys4(keys, start + r * stride, n);
+        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t k = kk[j];
+            uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+            uint32_t leader = __ffs(peers) - 1;
+            if (k != kInvalidKey && (threadIdx.x & 31u) == leader) atomicAdd(counts + k, (uint32_t)__popc(peers));
+        }
     }
 }
 
@@ -254,21 +268,26 @@ __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                       const uint2 *__restrict__ meta, uint32_t *__restrict__ cursor,
                                                       uint32_t *__restrict__ order) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
     const uint64_t rounds = (n + stride - 1) / stride;
     const uint32_t lane = threadIdx.x & 31u;
     for (uint64_t r = 0; r < rounds; ++r) {
-        uint64_t s = start + r * stride;
-        uint32_t k = s < n ? __ldg(keys + s) : kInvalidKey;
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-        uint32_t leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if (k != kInvalidKey && lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        if (k != kInvalidKey) {
-            uint32_t rank = __popc(peers & lanemask_lt());
-            order[__ldg(&meta[k].x) + base + rank] = (uint32_t)s;
+        const uint64_t s0 = start + r * stride;
+        const uint4 k4 = load_keys4(keys, s0, n);
+        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t k = kk[j];
+            uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+            uint32_t leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (k != kInvalidKey && lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            if (k != kInvalidKey) {
+                uint32_t rank = __popc(peers & lanemask_lt());
+                order[__ldg(&meta[k].x) + base + rank] = (uint32_t)(s0 + j);
+            }
         }
     }
 }
