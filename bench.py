@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -306,6 +307,212 @@ def photon_denoise_stages(steps: int, warmup: int, peak: float) -> dict:
     }
 
 
+# ------------------------------------------------------------------------------------------------
+# Many jobs: the batched form (64 jobs per frame) and the served form (Poisson arrivals)
+# ------------------------------------------------------------------------------------------------
+RESOLUTIONS = [(256, 256), (512, 512), (640, 480), (1280, 720)]
+SPPS = [1, 2, 4, 8, 16]
+
+
+def ico_level(tris: float) -> int:
+    """Subdivision level of the displaced icosphere closest (in log) to `tris` triangles: level L has
+    20 * 4^L, so the 10k - 2M range maps to levels 5 - 8 (20k, 82k, 328k, 1.3M)."""
+    return int(min(8, max(5, round(math.log(tris / 20.0, 4)))))
+
+
+def scene_pool(n: int, seed: int) -> list[tuple[int, object]]:
+    """n seeded icosphere rooms, triangle counts log-uniform in [10k, 2M], built on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import rustracer_gb300 as rt
+
+    rng = np.random.default_rng(seed)
+    levels = [ico_level(math.exp(rng.uniform(math.log(1e4), math.log(2e6)))) for _ in range(n)]
+    keys = [(lv, 1000 + i) for i, lv in enumerate(levels)]
+    with ThreadPoolExecutor(max_workers=min(n, os.cpu_count() or 1)) as ex:
+        scenes = list(ex.map(lambda k: rt.Scene.icosphere_room(k[0], k[1], 0.02, 1024), keys))
+    return list(zip(levels, scenes))
+
+
+def job_spec(rng, pool) -> dict:
+    """One render job as in the batched workload: scene drawn by triangle count (log-uniform in
+    [10k, 2M]) from the pool, resolution from RESOLUTIONS, spp from SPPS, depth 5-8, photon map on
+    half the jobs (2^18 - 2^20 photons), denoise on three quarters, a random camera orbit."""
+    level = ico_level(math.exp(rng.uniform(math.log(1e4), math.log(2e6))))
+    cands = [i for i, (lv, _) in enumerate(pool) if lv == level] or list(range(len(pool)))
+    w, h = RESOLUTIONS[int(rng.integers(len(RESOLUTIONS)))]
+    photons = int(2.0 ** rng.uniform(18, 20)) if rng.random() < 0.5 else 0
+    return dict(scene=int(cands[int(rng.integers(len(cands)))]), width=w, height=h,
+                spp=SPPS[int(rng.integers(len(SPPS)))], depth=int(rng.integers(5, 9)), photons=photons,
+                denoise=bool(rng.random() < 0.75), yaw=float(rng.uniform(-0.8, 0.8)),
+                pitch=float(rng.uniform(-0.3, 0.3)))
+
+
+def job_objects(spec: dict, pool):
+    import rustracer_gb300 as rt
+
+    scene = pool[spec["scene"]][1]
+    cfg = rt.RenderConfig(width=spec["width"], height=spec["height"], spp=spec["spp"], max_bounces=spec["depth"],
+                          accumulate_frames=0, enable_denoise=spec["denoise"],
+                          enable_photon_map=spec["photons"] > 0, photon_count=max(spec["photons"], 1))
+    cam = scene.default_camera()
+    cam.orbit(spec["yaw"], spec["pitch"])
+    return scene, cfg, cam
+
+
+def frame_launches(cfgs) -> int:
+    """Kernel launches of one batch frame over jobs with these configs: generate + finalize per job,
+    extend / shade / shadow per iteration, the counter kernel, then per job the denoise passes and
+    the resolve."""
+    iters = max(max(c.spp, 1) * (c.max_bounces or 6) for c in cfgs)
+    return 2 * len(cfgs) + 3 * iters + 1 + sum((c.denoise_passes or 2) * int(c.enable_denoise) + 1 for c in cfgs)
+
+
+def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> dict:
+    """64 jobs rendered (a) one job at a time with its own per-frame launches and (b) as one batch per
+    progressive frame captured as a CUDA graph.  Both render warmup + steps frames of every job from
+    a fresh renderer; the final accumulations are compared bit for bit (equal per-job RMSE)."""
+    import hashlib
+
+    import torch
+
+    import rustracer_gb300 as rt
+
+    rng = np.random.default_rng(seed)
+    specs = [job_spec(rng, pool) for _ in range(n_jobs)]
+    resident = {i: rt.ResidentScene(pool[i][1]) for i in sorted({s["scene"] for s in specs})}
+
+    def make(spec):
+        scene, cfg, cam = job_objects(spec, pool)
+        r = rt.Renderer(resident[spec["scene"]], cfg)
+        r.update_camera(cam)
+        if cfg.enable_photon_map:
+            r.rebuild_photons()
+        return r
+
+    digest = lambda r: hashlib.blake2b(r.read_accumulation().tobytes(), digest_size=16).hexdigest()  # noqa
+
+    # (a) plain: one job at a time
+    plain_s, plain_seg, plain_hash = 0.0, 0, []
+    for spec in specs:
+        r = make(spec)
+        r.render_frames(warmup)
+        r.synchronize()
+        s0 = r.stats()
+        t0 = time.perf_counter()
+        r.render_frames(steps)
+        r.synchronize()
+        plain_s += time.perf_counter() - t0
+        plain_seg += r.stats().segments - s0.segments
+        plain_hash.append(digest(r))
+        r.close()
+
+    # (b) batched: every job in each frame, one CUDA graph per progressive frame
+    rs = [make(spec) for spec in specs]
+    b = rt.Batch(rs, use_graphs=True)
+    b.render_frames(warmup)
+    b.synchronize()
+    s0 = b.stats()
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    b.render_frames(steps)
+    ev1.record(stream)
+    b.synchronize()
+    batch_s = time.perf_counter() - t0
+    batch_dev_ms = ev0.elapsed_time(ev1)
+    s1 = b.stats()
+    batch_seg = s1.segments - s0.segments
+    same = all(digest(r) == h for r, h in zip(rs, plain_hash))
+    b.close()
+    for r in rs:
+        r.close()
+    pixels = sum(s["width"] * s["height"] for s in specs)
+    plain_v, batch_v = plain_seg / plain_s, batch_seg / batch_s
+    return {
+        "workload": f"{n_jobs} jobs: icosphere rooms 10k-2M triangles (levels 5-8), resolutions {RESOLUTIONS}, "
+                    f"spp {SPPS}, depth 5-8, photon map on {sum(s['photons'] > 0 for s in specs)}, denoise on "
+                    f"{sum(s['denoise'] for s in specs)}; {pixels} pixels per frame",
+        "steps": steps, "warmup": warmup,
+        "plain_segments_per_s": plain_v,
+        "batched_segments_per_s": batch_v,
+        "batched_device_segments_per_s": batch_seg / (batch_dev_ms / 1000.0),
+        "speedup": batch_v / plain_v,
+        "segments_per_frame": batch_seg / steps,
+        "identical_outputs": bool(same and plain_seg == batch_seg),
+        "graph_captures": int(s1.graph_captures),
+        "gpu_launches_per_frame": frame_launches([job_objects(s, pool)[1] for s in specs]),
+        "resident_scenes": len(resident),
+    }
+
+
+def served_trace(rate: float, seconds: float, pool, seed: int) -> list[tuple[float, dict, int]]:
+    """Poisson arrivals at `rate` jobs/s for `seconds`: (arrival time, job spec, budget frames), the
+    budget log-uniform in [8, 256] frames."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > seconds:
+            return out
+        spec = job_spec(rng, pool)
+        spec["scene"] = int(rng.integers(len(pool)))  # requests spread over the whole pool
+        budget = int(round(math.exp(rng.uniform(math.log(8), math.log(256)))))
+        out.append((t, spec, budget))
+
+
+def served_arm(mode: str, trace, pool, seconds: float) -> dict:
+    import rustracer_gb300 as rt
+
+    srv = rt.Server(mode=mode, graphs=True, hbm_cap_bytes=120 << 30, max_jobs=64, max_slots=1 << 25)
+    for i, (_, sc) in enumerate(pool):
+        srv.add_scene(i, sc)
+    ids = []
+    s0 = srv.stats()
+    start = time.perf_counter()
+    for t_arr, spec, budget in trace:
+        delay = start + t_arr - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        _, cfg, cam = job_objects(spec, pool)
+        ids.append(srv.submit(spec["scene"], cfg, cam, budget))
+    rest = start + seconds - time.perf_counter()
+    if rest > 0:
+        time.sleep(rest)
+    wall = time.perf_counter() - start
+    st = srv.stats()
+    stats = [srv.status(j) for j in ids]
+    srv.close()  # finishes the frames in flight, drops the queue
+    ttff = [s.t_first_frame_ms - s.t_submit_ms for s in stats if s.t_first_frame_ms >= 0]
+    ttb = [s.t_done_ms - s.t_submit_ms for s in stats if s.state == rt._abi.JOB_DONE]
+    pct = lambda v, q: float(np.percentile(v, q)) if v else None  # noqa
+    return {
+        "segments_per_s": (st.segments - s0.segments) / wall,
+        "jobs_submitted": len(ids), "jobs_done": len(ttb), "jobs_started": len(ttff),
+        "ttff_ms": {"p50": pct(ttff, 50), "p95": pct(ttff, 95), "p99": pct(ttff, 99)},
+        "time_to_budget_ms": {"p50": pct(ttb, 50), "p95": pct(ttb, 95), "p99": pct(ttb, 99)},
+        "job_frames": int(st.job_frames), "batch_frames": int(st.batch_frames), "max_active": int(st.max_active),
+        "scene_uploads": int(st.scene_uploads), "scene_evictions": int(st.scene_evictions),
+        "graph_captures": int(st.graph_captures), "peak_device_bytes": int(st.peak_bytes),
+    }
+
+
+def served_leg(rate: float, seconds: float, pool, seed: int = 5) -> dict:
+    """The request loop under Poisson arrivals, continuous batching against the one-job-at-a-time
+    loop on the same arrival trace.  Percentiles are over the jobs that reached their first frame /
+    their budget inside the window (the rest are still queued when it closes)."""
+    trace = served_trace(rate, seconds, pool, seed)
+    batched = served_arm("batched", trace, pool, seconds)
+    plain = served_arm("plain", trace, pool, seconds)
+    return {
+        "workload": f"Poisson arrivals at {rate} jobs/s for {seconds} s over a pool of {len(pool)} scenes "
+                    f"(10k-2M triangles), budgets log-uniform in [8, 256] frames, HBM cap 120 GiB",
+        "batched": batched, "plain": plain,
+        "speedup": batched["segments_per_s"] / max(plain["segments_per_s"], 1e-9),
+    }
+
+
 def run_ours(args, w):
     import torch
 
@@ -410,6 +617,9 @@ def run_ours(args, w):
         achieved = algo / (gather_ms / 1000.0) / 1e9
         traffic = load_traffic(args.workload)
         stages = photon_denoise_stages(args.steps, args.warmup, peak) if args.stages else None
+        pool = scene_pool(32, 7) if (args.batched or args.served) else None
+        batched = batched_leg(args.batched_jobs, args.batched_steps, 2, pool) if args.batched else None
+        served = served_leg(args.served_rate, args.served_seconds, pool) if args.served else None
         line = {
             "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -417,7 +627,7 @@ def run_ours(args, w):
             "config": {"workload": args.workload, **{k: v for k, v in w.items()}, "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}"},
             "shadow_rays_per_s": shd_all / (ms_max / 1000.0),
-            "gpu_launches": int(2 * args.steps),
+            "gpu_launches": int(frame_launches([cfg]) * args.steps),
             "kernel_ms": {"gather": gather_ms, "resolve": resolve_ms},
             "roofline": {"bound": "hbm", "kernel": "gather_kernel", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -431,6 +641,8 @@ def run_ours(args, w):
                     "d2h_bytes_per_step": int(cfg.width * cfg.height * 4)},
             "clocks": clocks,
             "stages": stages,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(line), flush=True)
     r.close()
@@ -449,6 +661,12 @@ def main(argv=None) -> int:
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="size of the CPU-baseline sample")
     ap.add_argument("--no-stages", dest="stages", action="store_false",
                     help="skip the photon-map / denoise stage measurements")
+    ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the 64-job batch leg")
+    ap.add_argument("--batched-jobs", type=int, default=64)
+    ap.add_argument("--batched-steps", type=int, default=3)
+    ap.add_argument("--no-served", dest="served", action="store_false", help="skip the request-loop leg")
+    ap.add_argument("--served-rate", type=float, default=10.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--served-seconds", type=float, default=20.0, help="arrival window (s)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]

@@ -254,6 +254,7 @@ typedef struct rt_frame_stats {
     double ms_denoise_sum;
     double ms_resolve_sum;
     double ms_frame_sum;
+    uint64_t graph_captures;     /* batches: CUDA graphs captured so far                      */
 } rt_frame_stats;
 
 /* ---------------------------------------------------------------------------------------------
@@ -276,6 +277,25 @@ void rt_render_config_default(rt_render_config *cfg);
  * grid (lib.rs:416-457) and writes the derived photon_radius back into the renderer's config. */
 int rt_renderer_create(const rt_scene_desc *scene, const rt_render_config *cfg, rt_renderer **out);
 void rt_renderer_destroy(rt_renderer *r);
+
+/* Resident scenes (no counterpart in the reference, where each Renderer::new uploads its own copy):
+ * a scene's geometry, traversal layout, materials and textures uploaded once and shared by every
+ * renderer created on it.  Lights stay per renderer (rt_update_lights changes one renderer's copy).
+ * A resident scene is reference-counted: create returns one reference, each renderer on it holds
+ * one, and the device memory is freed with the last.  rt_renderer_create is create-resident +
+ * create-on + release. */
+typedef struct rt_resident_scene rt_resident_scene;
+int rt_resident_scene_create(const rt_scene_desc *scene, rt_resident_scene **out);
+void rt_resident_scene_release(rt_resident_scene *s);
+uint64_t rt_resident_scene_bytes(const rt_resident_scene *s);   /* device bytes held             */
+uint32_t rt_resident_scene_refs(const rt_resident_scene *s);    /* references (caller's + renderers') */
+int rt_renderer_create_resident(rt_resident_scene *s, const rt_render_config *cfg, rt_renderer **out);
+/* Device bytes the renderer owns now (frame, photon and path buffers; its scene not included). */
+uint64_t rt_renderer_device_bytes(const rt_renderer *r);
+/* Device bytes a renderer with this config on this scene allocates at create, and (optional) the
+ * path state its first solo frame adds; for admission by footprint before creating it. */
+int rt_renderer_footprint(const rt_render_config *cfg, const rt_resident_scene *s, uint64_t *create_bytes,
+                          uint64_t *solo_path_bytes);
 
 /* record_frame (lib.rs:666-851) minus the swapchain blit: gather -> [denoise x passes] ->
  * composite -> tonemap into the renderer's RGBA8 output buffer. */
@@ -325,6 +345,100 @@ int rt_read_photon_grid(rt_renderer *r, uint32_t *counts, uint32_t *meta, uint64
 /* Replaces the traced photon slots (n == photon_slots) and rebuilds the grid from them, skipping the
  * trace: lets a caller feed an identical photon buffer to this backend and to another one. */
 int rt_load_photons_and_build_grid(rt_renderer *r, const rt_photon *photons, uint64_t n);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched rendering (no counterpart in the reference, which renders one job per device): one call
+ * renders the next progressive frame of several renderers at once, the rays of every job sharing the
+ * same wavefront launches.  A job's image is identical alone and in a batch.  The renderers stay owned
+ * by the caller and must outlive the batch; do not render them alone while a batch frame is queued
+ * (read-backs on a renderer wait for the batch's work).  use_graphs != 0 captures each batch frame as
+ * a CUDA graph, replayed with the per-frame values (frame counters, cameras) read from device memory
+ * and captured again only when the launches' shape or baked settings change.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct rt_batch rt_batch;
+int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out);
+void rt_batch_destroy(rt_batch *b);
+int rt_batch_render_frame(rt_batch *b);
+int rt_batch_render_frames(rt_batch *b, uint32_t n);
+int rt_batch_synchronize(rt_batch *b);
+/* frames, segments / shadow rays of all jobs (cumulative), graph_captures; ms_frame_sum and
+ * timed_frames cover the batch frames since the previous call. */
+int rt_batch_get_stats(rt_batch *b, rt_frame_stats *out);
+void *rt_batch_stream(rt_batch *b);
+
+/* ---------------------------------------------------------------------------------------------
+ * The render-request loop (no counterpart in the reference, which renders one job per process):
+ * headless jobs of registered scenes are submitted as they arrive and rendered to their
+ * accumulation budgets by one worker thread that owns the server's CUDA work.
+ *   - RT_SERVER_BATCHED: continuous batching.  Every admitted job whose set-up is done is a member
+ *     of the next batch frame (rt_batch semantics); jobs join and leave between frames.  Jobs are
+ *     admitted in arrival order while max_jobs, max_slots (summed pixels) and hbm_cap_bytes allow.
+ *   - RT_SERVER_PLAIN: the same loop with one job at a time, rendered frame by frame alone with the
+ *     launches of rt_render_frame (max_jobs = 1, no graphs).
+ * A job's scene is uploaded on first use and stays resident after its jobs finish; when the cap
+ * would be exceeded, idle resident scenes (no admitted job) are freed least recently used first.
+ * The device bytes charged against the cap are the resident scenes, the admitted jobs' renderer
+ * buffers and the path state (max_slots x 192 B, reserved at create).  A job's image equals
+ * the image of the same request rendered alone by rt_renderer_create + rt_render_frame.
+ * Registered scene descriptions are borrowed: their arrays must stay valid and unchanged until
+ * rt_server_destroy.  submit / status / read_result / release / stats may be called from any thread.
+ * Times are milliseconds on the server's steady clock (0 at create); -1 where not reached yet.
+ * ------------------------------------------------------------------------------------------- */
+#define RT_SERVER_BATCHED 0u
+#define RT_SERVER_PLAIN 1u
+#define RT_JOB_QUEUED 0u
+#define RT_JOB_RUNNING 1u
+#define RT_JOB_DONE 2u
+#define RT_JOB_FAILED 3u
+
+typedef struct rt_server rt_server;
+typedef struct rt_server_config {
+    uint64_t hbm_cap_bytes;     /* 0: 120 GiB                                                    */
+    uint32_t max_jobs;          /* jobs rendered together (batched mode), 0: 64                   */
+    uint32_t max_slots;         /* summed pixels of the jobs rendered together, 0: 2^25           */
+    uint32_t mode;              /* RT_SERVER_BATCHED or RT_SERVER_PLAIN                            */
+    uint32_t graphs;            /* batched mode: capture a batch frame whose shape repeats        */
+    uint32_t frames_in_flight;  /* frames queued on the GPU ahead of the host, 0: 2               */
+    uint32_t _pad;
+} rt_server_config;
+typedef struct rt_request {
+    uint32_t scene_id;          /* as registered with rt_server_add_scene                         */
+    uint32_t budget_frames;     /* progressive frames to render (>= 1)                            */
+    uint32_t keep_result;       /* keep the final accumulation for rt_server_read_result          */
+    uint32_t _pad;
+    rt_render_config config;
+    rt_camera camera;
+} rt_request;
+typedef struct rt_job_status {
+    uint64_t job_id;
+    uint32_t state;             /* RT_JOB_*                                                        */
+    uint32_t frames_done;
+    double t_submit_ms, t_admit_ms, t_first_frame_ms, t_done_ms;
+} rt_job_status;
+typedef struct rt_server_stats {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t batch_frames;      /* frames launched (a batch frame counts once)                    */
+    uint64_t job_frames;        /* frames finished, summed over jobs                              */
+    uint64_t segments, shadow_rays;
+    uint64_t scene_uploads, scene_evictions, graph_captures;
+    uint64_t used_bytes, peak_bytes, resident_scene_bytes;
+    uint32_t active, pending, resident_scenes, max_active;
+} rt_server_stats;
+
+int rt_server_create(const rt_server_config *cfg, rt_server **out);
+/* Stops the worker after the frames in flight; queued jobs are dropped. */
+void rt_server_destroy(rt_server *s);
+int rt_server_add_scene(rt_server *s, uint32_t scene_id, const rt_scene_desc *scene);
+int rt_server_submit(rt_server *s, const rt_request *req, uint64_t *job_id);
+int rt_server_job_status(rt_server *s, uint64_t job_id, rt_job_status *out);
+/* The final accumulation (W*H*4 floats) of a done job submitted with keep_result. */
+int rt_server_read_result(rt_server *s, uint64_t job_id, float *rgba, uint64_t n_floats);
+/* Forgets a done or failed job (its status and kept result). */
+int rt_server_release_job(rt_server *s, uint64_t job_id);
+/* Waits until every submitted job is done or failed; RT_ERR_STATE after timeout_ms. */
+int rt_server_wait_idle(rt_server *s, uint32_t timeout_ms);
+int rt_server_get_stats(rt_server *s, rt_server_stats *out);
+double rt_server_now_ms(const rt_server *s);
 
 /* ---------------------------------------------------------------------------------------------
  * Stage entry points on caller-provided host buffers (copy in, run on the device, copy out).

@@ -37,6 +37,7 @@ NOALLOC_SCRATCH_BYTES = 9438208
 f3 = C.c_float * 3
 f4 = C.c_float * 4
 u32 = C.c_uint32
+u64 = C.c_uint64
 
 
 class BVHNode(C.Structure):
@@ -135,7 +136,35 @@ class FrameStats(C.Structure):
                 ("photons_stored", C.c_uint64), ("ms_gather", C.c_float), ("ms_denoise", C.c_float),
                 ("ms_resolve", C.c_float), ("ms_frame", C.c_float), ("ms_photon_trace", C.c_float),
                 ("ms_grid_build", C.c_float), ("timed_frames", C.c_uint64), ("ms_gather_sum", C.c_double),
-                ("ms_denoise_sum", C.c_double), ("ms_resolve_sum", C.c_double), ("ms_frame_sum", C.c_double)]
+                ("ms_denoise_sum", C.c_double), ("ms_resolve_sum", C.c_double), ("ms_frame_sum", C.c_double),
+                ("graph_captures", C.c_uint64)]
+
+
+SERVER_BATCHED, SERVER_PLAIN = 0, 1
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_cap_bytes", C.c_uint64), ("max_jobs", u32), ("max_slots", u32), ("mode", u32),
+                ("graphs", u32), ("frames_in_flight", u32), ("_pad", u32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", u32), ("budget_frames", u32), ("keep_result", u32), ("_pad", u32),
+                ("config", RenderConfigC), ("camera", Camera)]
+
+
+class JobStatus(C.Structure):
+    _fields_ = [("job_id", C.c_uint64), ("state", u32), ("frames_done", u32), ("t_submit_ms", C.c_double),
+                ("t_admit_ms", C.c_double), ("t_first_frame_ms", C.c_double), ("t_done_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "admitted", "completed", "failed", "batch_frames",
+                                          "job_frames", "segments", "shadow_rays", "scene_uploads",
+                                          "scene_evictions", "graph_captures", "used_bytes", "peak_bytes",
+                                          "resident_scene_bytes")] + \
+                [(n, u32) for n in ("active", "pending", "resident_scenes", "max_active")]
 
 
 def np_dtype(struct: type[C.Structure]) -> np.dtype:
@@ -176,6 +205,30 @@ _PROTOS: dict[str, tuple] = {
     "rt_read_sorted_photons": (C.c_int, [vp, vp, C.c_uint64]),
     "rt_read_photon_grid": (C.c_int, [vp, vp, vp, C.c_uint64]),
     "rt_load_photons_and_build_grid": (C.c_int, [vp, vp, C.c_uint64]),
+    "rt_resident_scene_create": (C.c_int, [P(SceneDesc), P(vp)]),
+    "rt_resident_scene_release": (None, [vp]),
+    "rt_resident_scene_bytes": (u64, [vp]),
+    "rt_resident_scene_refs": (u32, [vp]),
+    "rt_renderer_create_resident": (C.c_int, [vp, P(RenderConfigC), P(vp)]),
+    "rt_renderer_device_bytes": (u64, [vp]),
+    "rt_renderer_footprint": (C.c_int, [P(RenderConfigC), vp, P(u64), P(u64)]),
+    "rt_batch_create": (C.c_int, [P(vp), u32, u32, P(vp)]),
+    "rt_batch_destroy": (None, [vp]),
+    "rt_batch_render_frame": (C.c_int, [vp]),
+    "rt_batch_render_frames": (C.c_int, [vp, u32]),
+    "rt_batch_synchronize": (C.c_int, [vp]),
+    "rt_batch_get_stats": (C.c_int, [vp, P(FrameStats)]),
+    "rt_batch_stream": (vp, [vp]),
+    "rt_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
+    "rt_server_destroy": (None, [vp]),
+    "rt_server_add_scene": (C.c_int, [vp, u32, P(SceneDesc)]),
+    "rt_server_submit": (C.c_int, [vp, P(Request), P(u64)]),
+    "rt_server_job_status": (C.c_int, [vp, u64, P(JobStatus)]),
+    "rt_server_read_result": (C.c_int, [vp, u64, P(C.c_float), u64]),
+    "rt_server_release_job": (C.c_int, [vp, u64]),
+    "rt_server_wait_idle": (C.c_int, [vp, u32]),
+    "rt_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
+    "rt_server_now_ms": (C.c_double, [vp]),
     "rt_stage_denoise": (C.c_int, [vp, vp, vp, u32, u32, C.c_float, u32, vp]),
     "rt_stage_resolve": (C.c_int, [vp, vp, vp, u32, u32, C.c_float, P(TonemapParams), vp]),
     "rt_stage_photon_grid": (C.c_int, [vp, P(GridParams), vp, vp, vp]),

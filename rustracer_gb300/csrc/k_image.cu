@@ -15,7 +15,7 @@ __device__ __forceinline__ float luminance(f3 c) { return dot(c, mk3(0.2126f, 0.
 __global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__ in, float4 *__restrict__ out,
                                                       const float4 *__restrict__ gbuffer,
                                                       const float4 *__restrict__ moments,
-                                                      const rt_denoise_params p) {
+                                                      const rt_denoise_params p, const float *alpha_dev) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
     const uint32_t W = p.width, H = p.height;
@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__
             var_cnt += 1.0f;
         }
     const float var_frame = var_acc / fmaxf(var_cnt, 1.0f);
-    const float ema_scale = p.alpha / fmaxf(2.0f - p.alpha, 1e-4f);
+    const float alpha = alpha_dev ? *alpha_dev : p.alpha;
+    const float ema_scale = alpha / fmaxf(2.0f - alpha, 1e-4f);
     const float var_c = var_frame * ema_scale;
     const float denom_c = var_c * p.lambda + 1e-6f;
     const float denom_d = p.phi_depth * fmaxf(d_center, 1e-4f);
@@ -152,7 +153,8 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(cons
                                                                            float4 *__restrict__ out,
                                                                            const float4 *__restrict__ gbuffer,
                                                                            const float4 *__restrict__ moments,
-                                                                           const rt_denoise_params p) {
+                                                                           const rt_denoise_params p,
+                                                                           const float *alpha_dev) {
     constexpr int H = 2 * kStep, TW = kDnBX + 2 * H, TH = kDnRows + 2 * H;
     extern __shared__ float4 dn_smem[];
     float4(*s_cl)[TW] = reinterpret_cast<float4(*)[TW]>(dn_smem);
@@ -217,7 +219,8 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(cons
     const int ty = (int)threadIdx.y;
     const int r0 = (ty / kStep) * (kDnPix * kStep) + (ty % kStep);
     const int lx = (int)threadIdx.x, x = x0 + lx, y0 = y0t + r0;
-    const float ema_scale = p.alpha / fmaxf(2.0f - p.alpha, 1e-4f);
+    const float alpha = alpha_dev ? *alpha_dev : p.alpha;
+    const float ema_scale = alpha / fmaxf(2.0f - alpha, 1e-4f);
     float varc[kDnPix];
 #pragma unroll
     for (int k = 0; k < kDnPix; ++k) {
@@ -246,38 +249,42 @@ constexpr size_t denoise_smem_bytes() {
     return sizeof(float4) * 2 * (kDnBX + 4 * kStep) * (kDnRows + 4 * kStep) + sizeof(float) * (kDnBX + 2) * (kDnRows + 2);
 }
 
+void prepare_kernels() {
+    static bool done = false;  // opt in to more than 48 KB of dynamic shared memory, once per process
+    if (done) return;
+    cudaFuncSetAttribute(denoise_tiled_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)denoise_smem_bytes<1>());
+    cudaFuncSetAttribute(denoise_tiled_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)denoise_smem_bytes<2>());
+    done = true;
+}
+
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
-                           const rt_denoise_params &p, cudaStream_t st) {
+                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st) {
     if (p.step_size == 1u || p.step_size == 2u) {
-        static bool attr_set = false;  // opt in to more than 48 KB of dynamic shared memory, once
-        if (!attr_set) {
-            cudaFuncSetAttribute(denoise_tiled_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)denoise_smem_bytes<1>());
-            cudaFuncSetAttribute(denoise_tiled_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)denoise_smem_bytes<2>());
-            attr_set = true;
-        }
+        prepare_kernels();
         dim3 block(kDnBX, kDnThreadsY);
         dim3 grid((p.width + kDnBX - 1) / kDnBX, (p.height + kDnRows - 1) / kDnRows);
         if (p.step_size == 1u)
-            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(in, out, gbuffer, moments, p);
+            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(in, out, gbuffer, moments, p, alpha_dev);
         else
-            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(in, out, gbuffer, moments, p);
+            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(in, out, gbuffer, moments, p, alpha_dev);
         return cudaGetLastError();
     }
     dim3 block(32, 8);
     dim3 grid((p.width + block.x - 1) / block.x, (p.height + block.y - 1) / block.y);
-    denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p);
+    denoise_kernel<<<grid, block, 0, st>>>(in, out, gbuffer, moments, p, alpha_dev);
     return cudaGetLastError();
 }
 
 // composite.wgsl mix() then tonemap.wgsl, one pixel per thread, 1-D over the image.
 __global__ void __launch_bounds__(256) resolve_kernel(const float4 *__restrict__ frame, float4 *__restrict__ accum,
                                                       const float4 *__restrict__ gbuffer, uint32_t width,
-                                                      uint32_t npix, float alpha, const rt_tonemap_params tp,
-                                                      uchar4 *__restrict__ out) {
+                                                      uint32_t npix, float alpha_arg, const float *alpha_dev,
+                                                      const rt_tonemap_params tp, uchar4 *__restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npix) return;
+    const float alpha = alpha_dev ? *alpha_dev : alpha_arg;
     const float4 f = __ldg(frame + i);
     const float4 a = accum[i];
     // mix(prev, fresh, alpha) rounded as two products and a sum (no contraction: this file is
@@ -311,10 +318,12 @@ __global__ void __launch_bounds__(256) resolve_kernel(const float4 *__restrict__
 }
 
 cudaError_t launch_resolve(const float4 *frame, float4 *accum, const float4 *gbuffer, uint32_t width,
-                           uint32_t height, float alpha, const rt_tonemap_params &tp, uchar4 *out, cudaStream_t st) {
+                           uint32_t height, float alpha, const float *alpha_dev, const rt_tonemap_params &tp,
+                           uchar4 *out, cudaStream_t st) {
     const uint32_t npix = width * height;
     const uint32_t block = 256;
-    resolve_kernel<<<(npix + block - 1) / block, block, 0, st>>>(frame, accum, gbuffer, width, npix, alpha, tp, out);
+    resolve_kernel<<<(npix + block - 1) / block, block, 0, st>>>(frame, accum, gbuffer, width, npix, alpha, alpha_dev,
+                                                                 tp, out);
     return cudaGetLastError();
 }
 

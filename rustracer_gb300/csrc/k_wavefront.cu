@@ -110,8 +110,8 @@ struct LightSample {
     float max_dist;
     bool occlude;
 };
-__device__ __forceinline__ LightSample light_sample(const WaveParams &p, f3 hp, f3 sn, Rng &rng) {
-    const DevScene &s = p.scene;
+__device__ __forceinline__ LightSample light_sample(const DevJob &job, f3 hp, f3 sn, Rng &rng) {
+    const DevScene &s = job.scene;
     const uint32_t n = s.light_count;
     const f3 zero = mk3(0.0f, 0.0f, 0.0f);
     LightSample ls{zero, sn, zero, 0.0f, false};
@@ -127,7 +127,7 @@ __device__ __forceinline__ LightSample light_sample(const WaveParams &p, f3 hp, 
         f3 ld = to / r;
         ls.wi = ld;
         if (dot(sn, ld) <= 0.0f) return ls;
-        f3 pl = mk3(p.ip.point_light_emission[0], p.ip.point_light_emission[1], p.ip.point_light_emission[2]);
+        f3 pl = mk3(job.ip.point_light_emission[0], job.ip.point_light_emission[1], job.ip.point_light_emission[2]);
         ls.e = l.color * l.intensity * pl * fmaxf(dot(sn, ld), 0.0f) / (r2 + 0.01f) * fn;
         ls.o = hp + sn * 0.01f;
         ls.max_dist = r - 0.001f;
@@ -158,7 +158,7 @@ __device__ __forceinline__ LightSample light_sample(const WaveParams &p, f3 hp, 
             float4 t = tex_sample(s.tex[RT_TEX_EMISSIVE], uvx, uvy, (int32_t)mat.tex_emissive);
             le = le * mk3(t.x, t.y, t.z);
         }
-        le = le * mk3(p.ip.light_emission[0], p.ip.light_emission[1], p.ip.light_emission[2]);
+        le = le * mk3(job.ip.light_emission[0], job.ip.light_emission[1], job.ip.light_emission[2]);
         f3 to = lp - hp;
         float r2 = dot(to, to);
         float r = sqrtf(r2);
@@ -181,8 +181,8 @@ __device__ __forceinline__ LightSample light_sample(const WaveParams &p, f3 hp, 
 __device__ __forceinline__ int32_t clampi(int32_t x, int32_t lo, int32_t hi) { return x < lo ? lo : (x > hi ? hi : x); }
 
 // The camera ray of the pixel's next sample (gather.wgsl:292-297).
-__device__ __forceinline__ void camera_ray(const WaveParams &p, uint32_t px, uint32_t py, Rng &rng, f3 &ro, f3 &rd) {
-    const rt_camera_uniform &cam = p.cam;
+__device__ __forceinline__ void camera_ray(const DevJob &job, uint32_t px, uint32_t py, Rng &rng, f3 &ro, f3 &rd) {
+    const rt_camera_uniform &cam = job.cam;
     float jx = rng_f32(rng) - 0.5f;
     float jy = rng_f32(rng) - 0.5f;
     float ux = ((float)px + jx) * cam.inv_half_res[0] - 1.0f;
@@ -216,33 +216,36 @@ __device__ __forceinline__ uint32_t pack_sb(uint32_t s, uint32_t b) { return (s 
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------
-// generate: 8 x 4 pixel tiles, one per warp, so the first queue is tile-coherent.
+// generate: 8 x 4 pixel tiles, one per warp, so the first queue is tile-coherent.  One launch per job.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant__ WaveParams p) {
+__global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant__ WaveParams p, uint32_t jid) {
+    const DevJob &job = p.jobs[jid];
+    const uint32_t W = job.ip.width, H = job.ip.height;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t tiles_x = (p.ip.width + 7u) / 8u;
+    const uint32_t tiles_x = (W + 7u) / 8u;
     const uint32_t tile = blockIdx.x * 4u + warp;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     const uint32_t px = tx * 8u + (lane & 7u), py = ty * 4u + (lane >> 3);
-    const bool active = px < p.ip.width && py < p.ip.height;
-    uint32_t pix = 0;
+    const bool active = px < W && py < H;
+    uint32_t slot = 0;
     if (active) {
-        pix = py * p.ip.width + px;
-        uint32_t base_seed = pix + p.ip.frame * 2654435761u;
+        const uint32_t pix = py * W + px;
+        slot = job.base + pix;
+        uint32_t base_seed = pix + job.ip.frame * 2654435761u;
         Rng rng = rng_init(base_seed * 1664525u + 1013904223u);
         f3 ro, rd;
-        camera_ray(p, px, py, rng, ro, rd);
-        p.ro[pix] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
-        p.rd[pix] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(0u, 0u)));
-        p.thr[pix] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        camera_ray(job, px, py, rng, ro, rd);
+        p.ro[slot] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
+        p.rd[slot] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(0u, 0u)));
+        p.thr[slot] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(jid));
         const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        p.acc[4 * (size_t)pix] = z;
-        p.acc[4 * (size_t)pix + 1] = make_float4(0.0f, 1e30f, 0.0f, 0.0f);
-        p.acc[4 * (size_t)pix + 2] = z;
-        p.acc[4 * (size_t)pix + 3] = z;
-        p.nrm[pix] = make_float4(0.0f, 1.0f, 0.0f, 0.0f);
+        p.acc[4 * (size_t)slot] = z;
+        p.acc[4 * (size_t)slot + 1] = make_float4(0.0f, 1e30f, 0.0f, 0.0f);
+        p.acc[4 * (size_t)slot + 2] = z;
+        p.acc[4 * (size_t)slot + 3] = z;
+        p.nrm[slot] = make_float4(0.0f, 1.0f, 0.0f, 0.0f);
     }
-    warp_append(active, pix, p.queue[0], p.counts + 0);
+    warp_append(active, slot, p.queue[0], p.counts + 0);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -288,7 +291,7 @@ __device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n
     return mine;
 }
 
-// extend: closest hit of each queued path.
+// extend: closest hit of each queued path (any job: each lane traces its own job's scene).
 template <int kStack>
 __global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
     __shared__ uint32_t stack_smem[kStack * 128];
@@ -296,27 +299,27 @@ __global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ 
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
     uint32_t *fetch = p.counts + 4 * iter + 2;
-    const DevScene &s = p.scene;
     WarpFeed feed;
     TravState st;
     bool has = false;
-    uint32_t pix = 0;
+    uint32_t slot = 0;
     for (;;) {
         const uint32_t item = warp_take(feed, !has, n, fetch);
         if (item != 0xFFFFFFFFu) {
-            pix = q[item];
-            const float4 o = p.ro[pix], d = p.rd[pix];
-            st = trav_begin(xyz(o), xyz(d), kInf);
+            slot = q[item];
+            const float4 o = p.ro[slot], d = p.rd[slot];
+            const DevScene &sc = p.jobs[__float_as_uint(p.thr[slot].w)].scene;
+            st = trav_begin(sc, xyz(o), xyz(d), kInf);
             has = true;
-            if (s.cnode_count == 0u) {
-                p.hit[pix] = make_float2(kInf, 0.0f);
+            if (sc.cnode_count == 0u) {
+                p.hit[slot] = make_float2(kInf, 0.0f);
                 has = false;
             }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (int k = 0; k < kSteps && has; ++k) {
-            if (trav_step<false>(s, st, stk, 128u)) {
-                p.hit[pix] = make_float2(st.t, __uint_as_float(st.prim));
+            if (trav_step<false>(st, stk, 128u)) {
+                p.hit[slot] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
             }
         }
@@ -332,14 +335,6 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
     uint32_t *q_next = p.queue[(iter + 1u) & 1u];
     uint32_t *n_next = p.counts + 4 * (iter + 1u);
     uint32_t *n_shadow = p.counts + 4 * iter + 1u;
-    const DevScene &s = p.scene;
-    const rt_image_params &ip = p.ip;
-    const uint32_t W = ip.width;
-    const uint32_t spp = ip.spp > 1u ? ip.spp : 1u;
-    const uint32_t debug_view = ip._pad[0];
-    const float env_intensity = s.env_intensity;
-    const f3 env_color = mk3(s.env_color[0], s.env_color[1], s.env_color[2]);
-    const f3 env_horizon = mk3(s.env_horizon[0], s.env_horizon[1], s.env_horizon[2]);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounds = (n + stride - 1u) / stride;
 
@@ -348,24 +343,35 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
         const bool valid = i < n;
         bool keep = false;
         bool emit_shadow = false;
-        uint32_t pix = 0;
+        uint32_t slot = 0;
         f3 sh_o = mk3(0.0f, 0.0f, 0.0f), sh_d = sh_o, sh_c = sh_o;
         float sh_max = 0.0f;
         uint32_t sh_tag = 0;
         if (valid) {
-            pix = q[i];
+            slot = q[i];
+            const float4 o4 = p.ro[slot], d4 = p.rd[slot], t4 = p.thr[slot];
+            const uint32_t jid = __float_as_uint(t4.w);
+            const DevJob &job = p.jobs[jid];
+            const DevScene &s = job.scene;
+            const rt_image_params &ip = job.ip;
+            const uint32_t W = ip.width;
+            const uint32_t spp = job.spp;
+            const uint32_t debug_view = ip._pad[0];
+            const float env_intensity = s.env_intensity;
+            const f3 env_color = mk3(s.env_color[0], s.env_color[1], s.env_color[2]);
+            const f3 env_horizon = mk3(s.env_horizon[0], s.env_horizon[1], s.env_horizon[2]);
+            const uint32_t pix = slot - job.base;
             const uint32_t px = pix % W, py = pix / W;
-            const float4 o4 = p.ro[pix], d4 = p.rd[pix], t4 = p.thr[pix];
-            const float2 h2 = p.hit[pix];
+            const float2 h2 = p.hit[slot];
             f3 ro = xyz(o4), rd = xyz(d4), thr = xyz(t4);
             Rng rng{__float_as_uint(o4.w)};
             const uint32_t sb = __float_as_uint(d4.w);
             uint32_t sidx = sb & 0xFFFFu, b = sb >> 16;
             const float hit_t = h2.x;
             const uint32_t prim = __float_as_uint(h2.y);
-            Accum A = load_acc(p, pix);
-            float4 acc1 = p.acc[4 * (size_t)pix + 1];  // .y = first_depth
-            float4 nrm = p.nrm[pix];
+            Accum A = load_acc(p, slot);
+            float4 acc1 = p.acc[4 * (size_t)slot + 1];  // .y = first_depth
+            float4 nrm = p.nrm[slot];
             bool alive = true;  // the sample continues with another segment
 
             if (hit_t >= kInf) {
@@ -491,7 +497,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                         bool do_spec = rng_f32(rng) < spec_prob;
                         f3 dscale = diffuse_weight / (1.0f - spec_prob);
 
-                        LightSample ls = light_sample(p, hp, shn, rng);
+                        LightSample ls = light_sample(job, hp, shn, rng);
                         f3 c_nee;
                         if (!do_spec) {
                             if (env_intensity > 0.0f)
@@ -503,7 +509,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                         }
                         bool nee_luma_only = false;
                         if (ip.use_photons == 1u && !do_spec) {  // gather.wgsl:473-514
-                            const rt_grid_params &gp = p.gp;
+                            const rt_grid_params &gp = job.gp;
                             float r2 = ip.photon_radius * ip.photon_radius;
                             f3 ph_sum = mk3(0.0f, 0.0f, 0.0f);
                             uint32_t ph_hits = 0u, budget = 384u;
@@ -521,7 +527,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                                         int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
                                         uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x +
                                                         (uint32_t)cz * gp.grid_x * gp.grid_y;
-                                        uint2 m = __ldg(p.grid_meta + cell);
+                                        uint2 m = __ldg(job.grid_meta + cell);
                                         for (uint32_t k = 0; k < m.y && !done; ++k) {
                                             if (budget == 0u) {
                                                 done = true;
@@ -529,8 +535,8 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                                             }
                                             budget -= 1u;
                                             uint64_t idx = (uint64_t)m.x + k;
-                                            idx = idx < p.sorted_count ? idx : p.sorted_count - 1;
-                                            const float4 *ph = p.sorted_photons + 4ull * idx;
+                                            idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                                            const float4 *ph = job.sorted_photons + 4ull * idx;
                                             f3 dd = xyz(__ldg(ph)) - hp;
                                             float d2 = dot(dd, dd);
                                             if (d2 < r2) {
@@ -561,7 +567,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                             sh_d = ls.wi;
                             sh_c = c_nee;
                             sh_max = ls.max_dist;
-                            sh_tag = (sidx & 0xFFFFu) | (nee_luma_only ? 0x10000u : 0u);
+                            sh_tag = (sidx & 0xFFFFu) | (nee_luma_only ? 0x10000u : 0u) | (jid << 17);
                         }
                         if (do_spec) {
                             rd = sample_spec_dir(rd, shn, a, rng);
@@ -586,11 +592,11 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
             }
             // for-loop step: the segment index advances; the sample ends after max_bounces segments.
             b += 1u;
-            if (alive && b >= p.max_bounces) alive = false;
+            if (alive && b >= job.max_bounces) alive = false;
             if (!alive) {
                 sidx += 1u;
                 if (sidx < spp) {
-                    camera_ray(p, px, py, rng, ro, rd);
+                    camera_ray(job, px, py, rng, ro, rd);
                     thr = mk3(1.0f, 1.0f, 1.0f);
                     b = 0u;
                     keep = true;
@@ -598,11 +604,11 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
             } else {
                 keep = true;
             }
-            p.ro[pix] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
-            p.rd[pix] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(sidx, b)));
-            p.thr[pix] = make_float4(thr.x, thr.y, thr.z, 0.0f);
-            store_acc(p, pix, A, acc1);
-            p.nrm[pix] = nrm;
+            p.ro[slot] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
+            p.rd[slot] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(sidx, b)));
+            p.thr[slot] = make_float4(thr.x, thr.y, thr.z, __uint_as_float(jid));
+            store_acc(p, slot, A, acc1);
+            p.nrm[slot] = nrm;
         }
         // NEE shadow ray (deferred) and the continuing path.
         {
@@ -615,12 +621,12 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                 if (emit_shadow) {
                     float4 *rec = p.shadow + 3ull * (base + __popc(mask & lanemask_lt()));
                     rec[0] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_max);
-                    rec[1] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(pix));
+                    rec[1] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(slot));
                     rec[2] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sh_tag));
                 }
             }
         }
-        warp_append(keep, pix, q_next, n_next);
+        warp_append(keep, slot, q_next, n_next);
     }
 }
 
@@ -628,8 +634,9 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
 // shadow: the deferred NEE occlusion test (gather.wgsl:91-103) and the contribution of visible lights.
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec_i, const TravState &st, float limit) {
-    const DevScene &s = p.scene;
     const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1], c = p.shadow[3ull * rec_i + 2];
+    const uint32_t tag = __float_as_uint(c.w);
+    const DevScene &s = p.jobs[tag >> 17].scene;
     bool shadowed = !(st.t >= limit);
     if (shadowed && !s.any_hit_shadows) {
         TriFull bt = load_tri(s, st.prim);
@@ -640,13 +647,12 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
         }
     }
     if (shadowed) return;
-    const uint32_t pix = __float_as_uint(d.w);
-    const uint32_t tag = __float_as_uint(c.w);
-    Accum A = load_acc(p, pix);
-    const float4 acc1 = p.acc[4 * (size_t)pix + 1];
+    const uint32_t slot = __float_as_uint(d.w);
+    Accum A = load_acc(p, slot);
+    const float4 acc1 = p.acc[4 * (size_t)slot + 1];
     if (tag & 0x10000u) add_luma(tag & 0xFFFFu, A, xyz(c));
     else add_radiance(tag & 0xFFFFu, A, xyz(c));
-    store_acc(p, pix, A, acc1);
+    store_acc(p, slot, A, acc1);
 }
 
 template <int kStack>
@@ -655,10 +661,9 @@ __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ 
     uint32_t *stk = stack_smem + threadIdx.x;
     const uint32_t m = p.counts[4 * iter + 1];
     uint32_t *fetch = p.counts + 4 * iter + 3;
-    const DevScene &s = p.scene;
     WarpFeed feed;
     TravState st;
-    bool has = false;
+    bool has = false, any_hit = true;
     uint32_t rec_i = 0;
     float limit = 0.0f;
     for (;;) {
@@ -666,17 +671,21 @@ __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ 
         if (item != 0xFFFFFFFFu) {
             rec_i = item;
             const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1];
+            const DevScene &sc = p.jobs[__float_as_uint(p.shadow[3ull * rec_i + 2].w) >> 17].scene;
             limit = o.w - 0.001f;
             // Without cut-out materials the occlusion test may stop at the first triangle below the
             // limit; with them the reference's closest-hit-then-alpha rule is kept.
-            st = trav_begin(xyz(o), xyz(d), s.any_hit_shadows ? limit : kInf);
-            has = s.cnode_count != 0u;
-            if (!has) st.t = kInf;
-            if (!has) shadow_resolve(p, rec_i, st, limit);
+            any_hit = sc.any_hit_shadows != 0u;
+            st = trav_begin(sc, xyz(o), xyz(d), any_hit ? limit : kInf);
+            has = sc.cnode_count != 0u;
+            if (!has) {
+                st.t = kInf;
+                shadow_resolve(p, rec_i, st, limit);
+            }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (int k = 0; k < kSteps && has; ++k) {
-            const bool done = s.any_hit_shadows ? trav_step<true>(s, st, stk, 128u) : trav_step<false>(s, st, stk, 128u);
+            const bool done = any_hit ? trav_step<true>(st, stk, 128u) : trav_step<false>(st, stk, 128u);
             if (done) {
                 shadow_resolve(p, rec_i, st, limit);
                 has = false;
@@ -686,24 +695,17 @@ __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ 
 }
 
 // ------------------------------------------------------------------------------------------------
-// finalize: firefly sigma clamp and the frame outputs (gather.wgsl:548-593); segment counters.
+// finalize: firefly sigma clamp and the frame outputs (gather.wgsl:548-593).  One launch per job.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant__ WaveParams p, uint32_t iters) {
+__global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant__ WaveParams p, uint32_t jid) {
+    const DevJob &job = p.jobs[jid];
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix == 0u && p.counters) {
-        unsigned long long seg = 0, shd = 0;
-        for (uint32_t i = 0; i < iters; ++i) {
-            seg += p.counts[4 * i];
-            shd += p.counts[4 * i + 1];
-        }
-        atomicAdd(p.counters + 0, seg);
-        atomicAdd(p.counters + 1, shd);
-    }
-    if (pix >= p.npix) return;
-    const uint32_t spp = p.ip.spp > 1u ? p.ip.spp : 1u;
-    Accum A = load_acc(p, pix);
-    const float first_depth = p.acc[4 * (size_t)pix + 1].y;
-    const float4 nrm = p.nrm[pix];
+    if (pix >= job.npix) return;
+    const uint32_t slot = job.base + pix;
+    const uint32_t spp = job.spp;
+    Accum A = load_acc(p, slot);
+    const float first_depth = p.acc[4 * (size_t)slot + 1].y;
+    const float4 nrm = p.nrm[slot];
     if (spp <= 8u) {
         float *sl = A.sl;
         for (uint32_t i = 1; i < spp; ++i) {
@@ -735,23 +737,41 @@ __global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant_
         A.lum2_sum = cl2;
     }
     f3 col = vmin(A.col / (float)spp, mk3(10.0f, 10.0f, 10.0f));
-    p.frame[pix] = make_float4(col.x, col.y, col.z, 1.0f);
-    p.moments[pix] = make_float4(fminf(A.lum_sum / (float)spp, 10.0f), fminf(A.lum2_sum / (float)spp, 100.0f), 0.0f, 0.0f);
-    p.gbuffer[pix] = make_float4(nrm.x, nrm.y, nrm.z, first_depth);
+    job.frame[pix] = make_float4(col.x, col.y, col.z, 1.0f);
+    job.moments[pix] = make_float4(fminf(A.lum_sum / (float)spp, 10.0f), fminf(A.lum2_sum / (float)spp, 100.0f), 0.0f, 0.0f);
+    job.gbuffer[pix] = make_float4(nrm.x, nrm.y, nrm.z, first_depth);
+}
+
+// Segments (paths queued per iteration) and shadow rays of the pass, added to the 64-bit counters.
+__global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t iters) {
+    if (threadIdx.x != 0u || !p.counters) return;
+    unsigned long long seg = 0, shd = 0;
+    for (uint32_t i = 0; i < iters; ++i) {
+        seg += p.counts[4 * i];
+        shd += p.counts[4 * i + 1];
+    }
+    p.counters[0] += seg;
+    p.counters[1] += shd;
 }
 
 // ------------------------------------------------------------------------------------------------
-// Host launcher: the whole gather pass of one frame.
+// Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
-cudaError_t launch_wavefront(const WaveParams &p, uint32_t iters, int num_sms, cudaStream_t st) {
+cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
+                             cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4 * (size_t)(iters + 1), st)) != cudaSuccess) return e;
-    const uint32_t tiles = ((p.ip.width + 7u) / 8u) * ((p.ip.height + 3u) / 4u);
-    wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p);
-    const uint32_t blocks_needed = (p.npix + 127u) / 128u;
-    const uint32_t persistent = (uint32_t)num_sms * 8u;
-    const uint32_t grid = blocks_needed < persistent ? blocks_needed : persistent;
-    const bool big_stack = p.scene.stack_cap > 32u;
+    uint64_t slots = 0;
+    bool big_stack = false;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const uint32_t tiles = ((jobs[j].width + 7u) / 8u) * ((jobs[j].height + 3u) / 4u);
+        wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p, j);
+        slots += jobs[j].npix;
+        big_stack = big_stack || jobs[j].stack_cap > 32u;
+    }
+    const uint64_t blocks_needed = (slots + 127u) / 128u;
+    const uint64_t persistent = (uint64_t)num_sms * 8u;
+    const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);
     for (uint32_t it = 0; it < iters; ++it) {
         if (big_stack) wf_extend_kernel<64><<<grid, 128, 0, st>>>(p, it);
         else wf_extend_kernel<32><<<grid, 128, 0, st>>>(p, it);
@@ -759,7 +779,8 @@ cudaError_t launch_wavefront(const WaveParams &p, uint32_t iters, int num_sms, c
         if (big_stack) wf_shadow_kernel<64><<<grid, 128, 0, st>>>(p, it);
         else wf_shadow_kernel<32><<<grid, 128, 0, st>>>(p, it);
     }
-    wf_finalize_kernel<<<(p.npix + 255u) / 256u, 256, 0, st>>>(p, iters);
+    for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);
+    wf_count_kernel<<<1, 32, 0, st>>>(p, iters);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,290 @@
+// Batched rendering: one progressive frame of several renderers (render jobs) at once.  The rays of
+// every job share the wavefront's queues and launches (extend / shade / shadow run over all jobs'
+// paths together, each lane on its own job's scene), which keeps the GPU full when single jobs are
+// too small to.  Each job's per-pixel work is the one it does alone -- same seeds, same order of
+// operations -- so a job's image is the same bit for bit alone and in a batch.
+//
+// A batch frame can be captured as a CUDA graph and replayed: the per-frame values (frame counters,
+// cameras, accumulation alpha) live in the device job table, copied from pinned memory ahead of each
+// replay; the graph is captured again only when something baked into its launches changes (the
+// member jobs and their buffers, the number of iterations, the jobs' shapes, tonemap or denoise
+// settings).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "rt_batch_engine.h"
+
+using rt::set_error;
+
+namespace rt {
+
+namespace {
+
+template <class T>
+void put(std::vector<unsigned char> &v, const T &x) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(&x);
+    v.insert(v.end(), p, p + sizeof(T));
+}
+
+}  // namespace
+
+BatchEngine::~BatchEngine() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+int BatchEngine::init(uint32_t max_jobs, GraphMode mode) {
+    graph_mode = mode;
+    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+        set_error("batch: cannot create the stream");
+        return RT_ERR_CUDA;
+    }
+    if (jobs.init(max_jobs) != cudaSuccess || counters.alloc(64) != cudaSuccess ||
+        cudaMemset(counters.p, 0, 64) != cudaSuccess) {
+        set_error("batch: out of device memory for the job table");
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    num_sms = rtd::device_sm_count();
+    rtd::prepare_kernels();
+    return RT_OK;
+}
+
+int BatchEngine::reserve(uint64_t slots, uint32_t iters) {
+    if (slots > path.slots || sizeof(uint32_t) * 4 * ((size_t)iters + 1) > path.counts_bytes) {
+        RT_CK(cudaStreamSynchronize(stream));
+        RT_CK(path.ensure(slots, iters));
+    }
+    return RT_OK;
+}
+
+// Everything the frame's launches take by value (the job table itself is read from device memory).
+std::vector<unsigned char> BatchEngine::signature(rt_renderer *const *rs, uint32_t n, uint32_t iters) const {
+    std::vector<unsigned char> s;
+    put(s, iters);
+    put(s, n);
+    put(s, path.ro.p);
+    put(s, path.counts.p);
+    for (uint32_t j = 0; j < n; ++j) {
+        const rt_renderer *r = rs[j];
+        put(s, r);
+        put(s, r->d_frame.p);
+        put(s, r->d_pingpong.p);
+        put(s, r->d_moments.p);
+        put(s, r->d_gbuffer.p);
+        put(s, r->d_accum.p);
+        put(s, r->d_output.p);
+        put(s, r->cfg.width);
+        put(s, r->cfg.height);
+        put(s, r->cfg.enable_denoise);
+        put(s, r->cfg.denoise_passes);
+        put(s, r->cfg.exposure);
+        put(s, r->cfg.gamma);
+        put(s, r->scene.stack_cap);
+        put(s, r->glow);
+        put(s, r->marker);
+        put(s, base[j]);
+    }
+    return s;
+}
+
+int BatchEngine::enqueue(rt_renderer *const *rs, uint32_t n, uint32_t iters, const float *alpha, bool dev_alpha) {
+    std::vector<rtd::JobShape> shapes(n);
+    for (uint32_t j = 0; j < n; ++j) {
+        const rt_renderer *r = rs[j];
+        shapes[j] = rtd::JobShape{r->cfg.width, r->cfg.height, r->cfg.width * r->cfg.height, base[j],
+                                  r->scene.stack_cap};
+    }
+    const rtd::WaveParams wp = path.params(jobs.device(), n, counters.as<unsigned long long>());
+    RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, stream));
+    for (uint32_t j = 0; j < n; ++j)
+        if (int st = rt::enqueue_post(rs[j], alpha[j], dev_alpha ? &jobs.device()[j].alpha : nullptr, stream))
+            return st;
+    return RT_OK;
+}
+
+int BatchEngine::frame(rt_renderer *const *rs, uint32_t n) {
+    if (n == 0) return RT_OK;
+    if (n > jobs.cap) {
+        set_error("batch: %u jobs, the job table holds %zu", n, jobs.cap);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    // Work already queued on a member's own stream (set-up, photon rebuilds, solo frames) comes first.
+    for (uint32_t j = 0; j < n; ++j) {
+        RT_CK(cudaEventRecord(done, rs[j]->stream));
+        RT_CK(cudaStreamWaitEvent(stream, done, 0));
+    }
+    std::vector<float> alpha(n);
+    std::vector<rtd::DevJob> table(n);
+    base.resize(n);
+    uint32_t iters = 0;
+    uint64_t slots = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        base[j] = (uint32_t)slots;
+        slots += (uint64_t)rs[j]->cfg.width * rs[j]->cfg.height;
+        iters = std::max(iters, rt::frame_iterations(rs[j]));
+    }
+    if (slots > 0xFFFFFFFFull) {
+        set_error("batch: the jobs' pixels exceed 2^32");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    if (int st = reserve(slots, iters)) return st;
+    for (uint32_t j = 0; j < n; ++j) {
+        alpha[j] = rt::prepare_frame(rs[j]);
+        table[j] = rt::make_job(rs[j], base[j]);
+    }
+    cudaEvent_t fe[2] = {nullptr, nullptr};
+    for (auto &e : fe) RT_CK(ring.next(&e));
+    if (fe[1]) RT_CK(cudaEventRecord(fe[0], stream));
+    RT_CK(jobs.upload(table.data(), n, stream));
+    bool replay = false;
+    if (graph_mode != GraphMode::Off) {
+        std::vector<unsigned char> sig = signature(rs, n, iters);
+        if (exec && sig == this->sig) {
+            replay = true;
+        } else if (graph_mode == GraphMode::Always || sig == last_sig) {
+            if (exec) {
+                cudaGraphExecDestroy(exec);
+                exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            RT_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            int st = enqueue(rs, n, iters, alpha.data(), true);
+            cudaError_t ce = cudaStreamEndCapture(stream, &g);
+            if (st != RT_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            RT_CK(ce);
+            cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            RT_CK(ie);
+            this->sig.swap(sig);
+            captures += 1;
+            replay = true;
+        } else {
+            last_sig.swap(sig);  // captured if the next frame has the same shape
+        }
+    }
+    if (replay) RT_CK(cudaGraphLaunch(exec, stream));
+    else if (int st = enqueue(rs, n, iters, alpha.data(), false)) return st;
+    if (fe[1]) RT_CK(cudaEventRecord(fe[1], stream));
+    // Later work on each member's own stream (read-backs, solo frames, destroy) waits for this frame.
+    RT_CK(cudaEventRecord(done, stream));
+    for (uint32_t j = 0; j < n; ++j) {
+        RT_CK(cudaStreamWaitEvent(rs[j]->stream, done, 0));
+        rs[j]->frames += 1;
+    }
+    frames += 1;
+    return RT_OK;
+}
+
+int BatchEngine::stats(rt_frame_stats *out) {
+    std::memset(out, 0, sizeof(*out));
+    RT_CK(cudaStreamSynchronize(stream));
+    unsigned long long ctr[2] = {0, 0};
+    RT_CK(cudaMemcpy(ctr, counters.p, 16, cudaMemcpyDeviceToHost));
+    out->frames = frames;
+    out->segments = ctr[0];
+    out->shadow_rays = ctr[1];
+    out->graph_captures = captures;
+    const size_t groups = ring.used / 2;
+    for (size_t g = 0; g < groups; ++g) {
+        float v = 0.0f;
+        if (cudaEventElapsedTime(&v, ring.pool[2 * g], ring.pool[2 * g + 1]) == cudaSuccess)
+            out->ms_frame_sum += v;
+        else
+            cudaGetLastError();
+    }
+    out->timed_frames = groups;
+    ring.used = 0;
+    return RT_OK;
+}
+
+}  // namespace rt
+
+struct rt_batch {
+    std::vector<rt_renderer *> rs;
+    rt::BatchEngine eng;
+};
+
+extern "C" int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out) {
+    rt::clear_error();
+    if (!out || !renderers || n == 0 || n > (1u << 15)) {
+        set_error("rt_batch_create: need 1 .. 32768 renderers");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    rt_batch *b = new (std::nothrow) rt_batch();
+    if (!b) {
+        set_error("rt_batch_create: out of host memory");
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    auto fail = [&](int st) {
+        delete b;
+        return st;
+    };
+    uint64_t slots = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        if (!renderers[j]) {
+            set_error("rt_batch_create: renderer %u is null", j);
+            return fail(RT_ERR_INVALID_ARGUMENT);
+        }
+        for (uint32_t k = 0; k < j; ++k)
+            if (renderers[k] == renderers[j]) {
+                set_error("rt_batch_create: renderer %u appears twice", j);
+                return fail(RT_ERR_INVALID_ARGUMENT);
+            }
+        b->rs.push_back(renderers[j]);
+        slots += (uint64_t)renderers[j]->cfg.width * renderers[j]->cfg.height;
+        if (slots > 0xFFFFFFFFull) {
+            set_error("rt_batch_create: the jobs' pixels exceed 2^32");
+            return fail(RT_ERR_INVALID_ARGUMENT);
+        }
+    }
+    if (int st = b->eng.init(n, use_graphs ? rt::GraphMode::Always : rt::GraphMode::Off)) return fail(st);
+    *out = b;
+    return RT_OK;
+}
+
+extern "C" void rt_batch_destroy(rt_batch *b) { delete b; }
+
+extern "C" int rt_batch_render_frame(rt_batch *b) {
+    if (!b) {
+        set_error("rt_batch_render_frame: null batch");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    rt::clear_error();
+    return b->eng.frame(b->rs.data(), (uint32_t)b->rs.size());
+}
+
+extern "C" int rt_batch_render_frames(rt_batch *b, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i)
+        if (int st = rt_batch_render_frame(b)) return st;
+    return RT_OK;
+}
+
+extern "C" int rt_batch_synchronize(rt_batch *b) {
+    if (!b) {
+        set_error("rt_batch_synchronize: null batch");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    RT_CK(cudaStreamSynchronize(b->eng.stream));
+    return RT_OK;
+}
+
+extern "C" void *rt_batch_stream(rt_batch *b) { return b ? (void *)b->eng.stream : nullptr; }
+
+extern "C" int rt_batch_get_stats(rt_batch *b, rt_frame_stats *out) {
+    if (!b || !out) {
+        set_error("rt_batch_get_stats: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    return b->eng.stats(out);
+}

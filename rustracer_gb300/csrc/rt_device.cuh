@@ -272,10 +272,15 @@ struct TravState {
     f3 ro, rd, inv;
     float t;
     uint32_t prim, node, sp;
+    const float4 *cnodes, *tri_ord;  // the traversal layout of the ray's scene
+    uint32_t cap;                    // stack entries this scene may use
 };
 
-__device__ __forceinline__ TravState trav_begin(f3 ro, f3 rd, float t_limit) {
+__device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd, float t_limit) {
     TravState st;
+    st.cnodes = s.cnodes;
+    st.tri_ord = s.tri_ord;
+    st.cap = s.stack_cap;
     st.ro = ro;
     st.rd = rd;
     st.inv = mk3(1.0f, 1.0f, 1.0f) / rd;
@@ -289,8 +294,8 @@ __device__ __forceinline__ TravState trav_begin(f3 ro, f3 rd, float t_limit) {
 // Visits one record.  Returns true when the traversal has finished (st.t / st.prim hold the result;
 // for kAny, st.t < the limit means an occluder was found).
 template <bool kAny>
-__device__ __forceinline__ bool trav_step(const DevScene &s, TravState &st, uint32_t *stk, uint32_t stride) {
-    const float4 *np = s.cnodes + 4ull * st.node;
+__device__ __forceinline__ bool trav_step(TravState &st, uint32_t *stk, uint32_t stride) {
+    const float4 *np = st.cnodes + 4ull * st.node;
     const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
     const f3 ro = st.ro, rd = st.rd, inv = st.inv;
     const f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
@@ -310,7 +315,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &s, TravState &st, uint
         if (h && cnt) {
             const uint32_t first = side == 0 ? lref : rref;
             for (uint32_t k = 0; k < cnt; ++k) {
-                const float4 *tp = s.tri_ord + 3ull * (first + k);
+                const float4 *tp = st.tri_ord + 3ull * (first + k);
                 const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
                 // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
                 const f3 h3 = cross(rd, xyz(e2));
@@ -343,7 +348,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &s, TravState &st, uint
         const bool left_first = le <= re;
         const uint32_t far = left_first ? rref : lref;
         st.node = left_first ? lref : rref;
-        if (st.sp < s.stack_cap) {
+        if (st.sp < st.cap) {
             stk[st.sp * stride] = far;
             st.sp += 1u;
         }
@@ -363,9 +368,9 @@ template <bool kAny>
 __device__ __forceinline__ Hit trace(const DevScene &s, f3 ro, f3 rd, float t_limit, uint32_t *stk,
                                      uint32_t stride) {
     if (s.cnode_count == 0u) return Hit{kInf, 0u};
-    TravState st = trav_begin(ro, rd, t_limit);
+    TravState st = trav_begin(s, ro, rd, t_limit);
     bool found = false;
-    while (!trav_step<kAny>(s, st, stk, stride)) {
+    while (!trav_step<kAny>(st, stk, stride)) {
     }
     if (kAny) found = st.t < t_limit;
     if (kAny) return Hit{found ? st.t : kInf, st.prim};

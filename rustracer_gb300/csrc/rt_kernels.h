@@ -8,8 +8,9 @@
 
 namespace rtd {
 
-// The wavefront gather pass.  Path state has one slot per pixel (slot == pixel index).
-struct WaveParams {
+// One render job of the wavefront (a renderer's frame).  The table lives in device memory so the
+// per-frame values (frame counter, camera) are read there, not baked into launch parameters.
+struct DevJob {
     DevScene scene;
     rt_camera_uniform cam;
     rt_image_params ip;
@@ -17,24 +18,39 @@ struct WaveParams {
     const float4 *sorted_photons;  // 4 x float4 per photon
     uint64_t sorted_count;
     const uint2 *grid_meta;        // (start, count) per cell
-    uint32_t max_bounces, npix;
-    float4 *ro;        // origin, .w = RNG state
-    float4 *rd;        // direction, .w = sample index | segment index << 16
-    float4 *thr;       // throughput
-    float2 *hit;       // closest t, primitive
-    float4 *acc;       // 4 per pixel: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
-    float4 *nrm;       // first-hit shading normal
-    uint32_t *queue[2];
-    uint32_t *counts;  // per iteration: [0] paths queued, [1] shadow rays
-    float4 *shadow;    // 3 per deferred NEE ray: (origin, max_dist), (dir, pixel), (contribution, tag)
+    uint32_t max_bounces, npix, base, spp;  // base: first path slot; spp = max(1, ip.spp)
     float4 *frame;
     float4 *moments;
     float4 *gbuffer;
+    float alpha;  // the frame's accumulation alpha, read by denoise and resolve in a replayed graph
+};
+
+// The wavefront gather pass over one or more jobs.  Path state has one slot per pixel of every job
+// (slot = job.base + pixel); queues hold slots of any job.
+struct WaveParams {
+    const DevJob *jobs;
+    uint32_t n_jobs;
+    float4 *ro;        // origin, .w = RNG state
+    float4 *rd;        // direction, .w = sample index | segment index << 16
+    float4 *thr;       // throughput, .w = job index
+    float2 *hit;       // closest t, primitive
+    float4 *acc;       // 4 per slot: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
+    float4 *nrm;       // first-hit shading normal
+    uint32_t *queue[2];
+    uint32_t *counts;  // per iteration: [0] paths queued, [1] shadow rays, [2] / [3] fetch cursors
+    float4 *shadow;    // 3 per deferred NEE ray: (origin, max_dist), (dir, slot), (contribution, tag)
     unsigned long long *counters;  // [0] segments, [1] shadow rays (cumulative)
 };
-// generate, spp * max_bounces iterations of extend / shade / shadow, finalize.
-cudaError_t launch_wavefront(const WaveParams &p, uint32_t iters, int num_sms, cudaStream_t st);
+// Host-side shape of a job for the per-job launches.
+struct JobShape {
+    uint32_t width, height, npix, base, stack_cap;
+};
+// generate (per job), iters x (extend, shade, shadow) over all jobs, finalize (per job), counters.
+cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
+                             cudaStream_t st);
 int device_sm_count();
+// One-time kernel attributes (shared-memory opt-ins); call before capturing launches into a graph.
+void prepare_kernels();
 
 struct PhotonTraceParams {
     DevScene scene;
@@ -70,10 +86,13 @@ cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const
 cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st);
 
 // Image kernels.
+// alpha_dev, when not null, is read on the device in place of p.alpha (a CUDA graph replays the
+// launch with the value of the frame being replayed).
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
-                           const rt_denoise_params &p, cudaStream_t st);
-// accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass.
+                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st);
+// accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass; alpha_dev as above.
 cudaError_t launch_resolve(const float4 *frame, float4 *accum, const float4 *gbuffer, uint32_t width,
-                           uint32_t height, float alpha, const rt_tonemap_params &tp, uchar4 *out, cudaStream_t st);
+                           uint32_t height, float alpha, const float *alpha_dev, const rt_tonemap_params &tp,
+                           uchar4 *out, cudaStream_t st);
 
 }  // namespace rtd

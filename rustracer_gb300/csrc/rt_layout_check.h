@@ -52,3 +52,12 @@ static_assert(offsetof(rt_grid_params, grid_x) == 16 && offsetof(rt_grid_params,
 static_assert(sizeof(rt_denoise_params) == 32, "DenoiseParamsUniform is 32 bytes");
 static_assert(sizeof(rt_composite_params) == 16, "CompositeParams is 16 bytes");
 static_assert(sizeof(rt_tonemap_params) == 32 && offsetof(rt_tonemap_params, marker) == 16, "ToneMapUniform");
+
+// Backend-only structs (no reference counterpart): sizes the ctypes mirror relies on.
+static_assert(sizeof(rt_render_config) == 96, "rt_render_config");
+static_assert(sizeof(rt_camera) == 52, "rt_camera");
+static_assert(sizeof(rt_server_config) == 32, "rt_server_config");
+static_assert(sizeof(rt_request) == 164 && offsetof(rt_request, config) == 16 && offsetof(rt_request, camera) == 112,
+              "rt_request");
+static_assert(sizeof(rt_job_status) == 48, "rt_job_status");
+static_assert(sizeof(rt_server_stats) == 128, "rt_server_stats");

@@ -13,127 +13,17 @@
 //           counts / cursor / (start, count) per cell, scan partials.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
 
-#include "rt_internal.h"
-#include "rt_kernels.h"
+#include "rt_renderer_impl.h"
 
+using rt::DevBuf;
 using rt::set_error;
-
-namespace {
-
-#define RT_CK(call)                                                                                    \
-    do {                                                                                               \
-        cudaError_t e_ = (call);                                                                       \
-        if (e_ != cudaSuccess) {                                                                       \
-            set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);     \
-            return e_ == cudaErrorMemoryAllocation ? RT_ERR_OUT_OF_MEMORY : RT_ERR_CUDA;               \
-        }                                                                                              \
-    } while (0)
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    cudaError_t alloc(size_t n) {
-        release();
-        if (n == 0) n = 16;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        else p = nullptr;
-        return e;
-    }
-    template <class T>
-    T *as() const {
-        return reinterpret_cast<T *>(p);
-    }
-};
-
-struct Events {
-    cudaEvent_t ev[8] = {};
-    ~Events() {
-        for (auto &e : ev)
-            if (e) cudaEventDestroy(e);
-    }
-    cudaError_t create() {
-        for (auto &e : ev) {
-            cudaError_t r = cudaEventCreate(&e);
-            if (r != cudaSuccess) return r;
-        }
-        return cudaSuccess;
-    }
-};
-enum { EV_FRAME0 = 0, EV_GATHER1, EV_DENOISE1, EV_RESOLVE1, EV_TRACE0, EV_TRACE1, EV_GRID1 };
-
-}  // namespace
-
-// Four events per frame (frame start, gather end, denoise end, resolve end), pooled; drained by
-// rt_get_stats.
-struct FrameEventRing {
-    std::vector<cudaEvent_t> pool;
-    size_t used = 0;  // events handed out since the last drain
-    ~FrameEventRing() {
-        for (auto e : pool) cudaEventDestroy(e);
-    }
-    cudaError_t next(cudaEvent_t *out) {
-        if (used == pool.size()) {
-            if (pool.size() >= (1u << 16)) {  // bounded: oldest timings are dropped past 16k frames
-                *out = nullptr;
-                return cudaSuccess;
-            }
-            cudaEvent_t e;
-            cudaError_t r = cudaEventCreate(&e);
-            if (r != cudaSuccess) return r;
-            pool.push_back(e);
-        }
-        *out = pool[used++];
-        return cudaSuccess;
-    }
-};
-
-struct rt_renderer {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    rt_render_config cfg{};
-    rt_grid_params gp{};
-    rt_camera_uniform cam{};
-    std::vector<rt_light> lights_host;
-    rtd::DevScene scene{};
-    DevBuf d_cnodes, d_tri_ord, d_tris, d_mats, d_lights, d_tex[4];
-    DevBuf d_frame, d_pingpong, d_moments, d_gbuffer, d_accum, d_output;
-    // wavefront path state (one slot per pixel)
-    DevBuf w_ro, w_rd, w_thr, w_hit, w_acc, w_nrm, w_queue[2], w_shadow, w_counts;
-    size_t w_counts_bytes = 0;
-    int num_sms = 1;
-    DevBuf d_photons, d_keys, d_order, d_sorted, d_counts, d_meta, d_cursor, d_partials, d_total, d_counters;
-    uint64_t photon_slots = 1;
-    bool photon_buffers = false;
-    uint32_t sample_counter = 0, frames_since_reset = 0;
-    float marker[4] = {0, 0, 0, 0};
-    float glow = 1.0f;
-    uint64_t frames = 0;
-    bool have_frame_timing = false, have_photon_timing = false;
-    uint32_t last_denoise_passes = 0;
-    Events events;
-    FrameEventRing ring;
-    ~rt_renderer() {
-        if (stream) {
-            cudaStreamSynchronize(stream);
-            cudaStreamDestroy(stream);
-        }
-    }
-};
+using namespace rt;  // EV_* event slots
 
 namespace {
 
@@ -211,36 +101,49 @@ extern "C" int rt_device_count(void) {
     return n;
 }
 
-extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_config *cfg, rt_renderer **out) {
-    rt::clear_error();
-    if (!sd || !cfg || !out) {
-        set_error("rt_renderer_create: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    if (cfg->width == 0 || cfg->height == 0 || (uint64_t)cfg->width * cfg->height > (1ull << 28)) {
-        set_error("rt_renderer_create: width/height must be non-zero and width*height <= 2^28");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
+namespace {
+
+int check_scene_desc(const rt_scene_desc *sd, const char *fn) {
     if ((sd->triangle_count && !sd->triangles) || (sd->bvh_node_count && !sd->bvh_nodes) ||
         (sd->bvh_prim_count && !sd->bvh_prims) || (sd->material_count && !sd->materials) ||
         (sd->light_count && !sd->lights)) {
-        set_error("rt_renderer_create: scene array pointer is null with a non-zero count");
+        set_error("%s: scene array pointer is null with a non-zero count", fn);
         return RT_ERR_INVALID_ARGUMENT;
     }
     if (sd->bvh_node_count && (sd->triangle_count == 0 || sd->material_count == 0 || sd->bvh_prim_count == 0)) {
-        set_error("rt_renderer_create: a BVH needs triangles, prim indices and at least one material");
+        set_error("%s: a BVH needs triangles, prim indices and at least one material", fn);
         return RT_ERR_INVALID_ARGUMENT;
     }
     if (sd->triangle_count > 0xFFFFFFFFull || sd->bvh_node_count > 0xFFFFFFFFull || sd->bvh_prim_count > 0xFFFFFFFFull ||
         sd->material_count > 0xFFFFFFFFull || sd->light_count > 0xFFFFFFFFull) {
-        set_error("rt_renderer_create: scene arrays are limited to 2^32 - 1 elements");
+        set_error("%s: scene arrays are limited to 2^32 - 1 elements", fn);
         return RT_ERR_INVALID_ARGUMENT;
     }
     if (rt_device_count() <= 0) {
-        set_error("rt_renderer_create: no CUDA device is visible");
+        set_error("%s: no CUDA device is visible", fn);
         return RT_ERR_CUDA;
     }
+    return RT_OK;
+}
+
+int check_config(const rt_render_config *cfg, const char *fn) {
+    if (cfg->width == 0 || cfg->height == 0 || (uint64_t)cfg->width * cfg->height > (1ull << 28)) {
+        set_error("%s: width/height must be non-zero and width*height <= 2^28", fn);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    if (cfg->enable_photon_map && (uint64_t)cfg->photon_count * RT_MAX_BOUNCES > 0xFFFFFFFFull) {
+        set_error("%s: photon_count * 6 must fit in 32 bits", fn);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    return RT_OK;
+}
+
+uint64_t photon_slots_of(const rt_render_config &c) {
+    return c.enable_photon_map ? std::max<uint64_t>((uint64_t)c.photon_count * RT_MAX_BOUNCES, 1) : 1;
+}
+
+// The renderer's own buffers on a resident scene (Renderer::new after the scene upload).
+int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer **out) {
     rt_renderer *r = new (std::nothrow) rt_renderer();
     if (!r) {
         set_error("rt_renderer_create: out of host memory");
@@ -250,8 +153,14 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
         delete r;
         return st;
     };
-    int st;
     cudaGetDevice(&r->device);
+    if (r->device != res->device) {
+        set_error("rt_renderer_create: the resident scene lives on device %d, the current device is %d",
+                  res->device, r->device);
+        return fail(RT_ERR_INVALID_ARGUMENT);
+    }
+    res->refs.fetch_add(1);
+    r->res = res;
     if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess) {
         set_error("rt_renderer_create: cudaStreamCreate failed");
         return fail(RT_ERR_CUDA);
@@ -262,47 +171,13 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
     }
     r->cfg = *cfg;
     cudaStream_t s = r->stream;
-
-    // Scene upload (Renderer::new, lib.rs:234-266).
-    if ((st = upload(r->d_tris, sd->triangles, sd->triangle_count, s)) != RT_OK) return fail(st);
-    rt::TraversalLayout lay;
-    if (!rt::build_traversal_layout(sd->bvh_nodes, sd->bvh_node_count, sd->bvh_prims, sd->bvh_prim_count,
-                                    sd->triangles, sd->triangle_count, lay))
-        return fail(RT_ERR_INVALID_ARGUMENT);
-    if ((st = upload(r->d_cnodes, lay.cnodes.data(), lay.cnodes.size(), s)) != RT_OK) return fail(st);
-    if ((st = upload(r->d_tri_ord, lay.tri_ord.data(), lay.tri_ord.size(), s)) != RT_OK) return fail(st);
-    // Host copies of the layout are freed when `lay` goes out of scope; wait for the copies first.
-    RT_CK(cudaStreamSynchronize(s));
-    if ((st = upload(r->d_mats, sd->materials, sd->material_count, s)) != RT_OK) return fail(st);
-    if ((st = upload(r->d_lights, sd->lights, sd->light_count, s)) != RT_OK) return fail(st);
-    r->lights_host.assign(sd->lights, sd->lights + sd->light_count);
-    rtd::DevScene &ds = r->scene;
-    ds.cnodes = r->d_cnodes.as<float4>();
-    ds.tri_ord = r->d_tri_ord.as<float4>();
-    ds.cnode_count = (uint32_t)(lay.cnodes.size() / 16);
-    // A near-first traversal holds at most one pending entry per tree level.
-    ds.stack_cap = lay.max_depth < 32u ? 32u : 63u;
-    ds.any_hit_shadows = 1u;
-    for (uint64_t i = 0; i < sd->material_count; ++i)
-        if ((sd->materials[i].flags & RT_MAT_FLAG_ALPHA_CUTOUT) && sd->materials[i].tex_albedo != RT_TEX_NONE)
-            ds.any_hit_shadows = 0u;
-    ds.tris = r->d_tris.as<float4>();
-    ds.mats = r->d_mats.as<float4>();
-    ds.lights = r->d_lights.as<float4>();
-    ds.tri_count = (uint32_t)sd->triangle_count;
-    ds.mat_count = (uint32_t)sd->material_count;
-    ds.light_count = (uint32_t)sd->light_count;
-    const rt_texture_array *roles[4] = {&sd->tex_albedo, &sd->tex_mr, &sd->tex_emissive, &sd->tex_normal};
-    for (int i = 0; i < 4; ++i) {
-        const rt_texture_array &t = *roles[i];
-        if (t.rgba8 && t.layers && t.width && t.height) {
-            size_t bytes = (size_t)t.width * t.height * t.layers * 4;
-            if ((st = upload(r->d_tex[i], t.rgba8, bytes, s)) != RT_OK) return fail(st);
-            ds.tex[i] = rtd::DevTex{r->d_tex[i].as<uchar4>(), t.width, t.height, t.layers};
-        } else {
-            ds.tex[i] = rtd::DevTex{nullptr, 0, 0, 0};
-        }
-    }
+    int st;
+    // Lights are per renderer (update_lights changes them); the rest of the scene is shared.
+    r->lights_host = res->lights;
+    if ((st = upload(r->d_lights, res->lights.data(), res->lights.size(), s)) != RT_OK) return fail(st);
+    r->scene = res->scene;
+    r->scene.lights = r->d_lights.as<float4>();
+    r->scene.light_count = (uint32_t)res->lights.size();
     resolve_env(r);
 
     // Camera::default().to_uniform (lib.rs:267-271).
@@ -320,19 +195,9 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
         }
         RT_CK(cudaMemsetAsync(b->p, 0, npix * 16, s));
     }
-    {
-        DevBuf *wb[6] = {&r->w_ro, &r->w_rd, &r->w_thr, &r->w_nrm, &r->w_hit, &r->w_acc};
-        const size_t wsz[6] = {16, 16, 16, 16, 8, 64};
-        for (int i = 0; i < 6; ++i)
-            if (wb[i]->alloc(npix * wsz[i]) != cudaSuccess) {
-                set_error("rt_renderer_create: out of device memory for path state");
-                return fail(RT_ERR_OUT_OF_MEMORY);
-            }
-        if (r->w_queue[0].alloc(npix * 4) != cudaSuccess || r->w_queue[1].alloc(npix * 4) != cudaSuccess ||
-            r->w_shadow.alloc(npix * 48) != cudaSuccess) {
-            set_error("rt_renderer_create: out of device memory for ray queues");
-            return fail(RT_ERR_OUT_OF_MEMORY);
-        }
+    if (r->jobs.init(1) != cudaSuccess) {
+        set_error("rt_renderer_create: cannot allocate the job table");
+        return fail(RT_ERR_OUT_OF_MEMORY);
     }
     r->num_sms = rtd::device_sm_count();
     RT_CK(r->d_output.alloc(npix * 4));
@@ -342,13 +207,9 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
 
     // Photon grid (lib.rs:276-286, 416-481).
     r->photon_buffers = cfg->enable_photon_map != 0;
-    r->photon_slots = r->photon_buffers ? std::max<uint64_t>((uint64_t)cfg->photon_count * RT_MAX_BOUNCES, 1) : 1;
-    if (r->photon_slots > 0xFFFFFFFFull) {
-        set_error("rt_renderer_create: photon_count * 6 must fit in 32 bits");
-        return fail(RT_ERR_INVALID_ARGUMENT);
-    }
+    r->photon_slots = photon_slots_of(*cfg);
     float radius = cfg->photon_radius;
-    rt_derive_grid(sd->bounds_min, sd->bounds_max, (int)sd->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
+    rt_derive_grid(res->bmin, res->bmax, (int)res->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
                    (uint32_t)r->photon_slots, &r->gp, &radius);
     r->cfg.photon_radius = radius;
     const uint64_t S = r->photon_slots, C = r->gp.num_cells;
@@ -373,64 +234,230 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
     return RT_OK;
 }
 
+}  // namespace
+
+rt_renderer::~rt_renderer() {
+    if (stream) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+    if (res) rt::resident_scene_release(res);
+}
+
+uint64_t rt_renderer::device_bytes() const {
+    uint64_t n = d_lights.bytes + d_frame.bytes + d_pingpong.bytes + d_moments.bytes + d_gbuffer.bytes +
+                 d_accum.bytes + d_output.bytes + d_photons.bytes + d_keys.bytes + d_order.bytes + d_sorted.bytes +
+                 d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
+                 d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
+    const rt::DevBuf *pb[10] = {&path.ro, &path.rd, &path.thr, &path.hit, &path.acc,
+                                &path.nrm, &path.queue[0], &path.queue[1], &path.shadow, &path.counts};
+    for (int i = 0; i < 9; ++i) n += pb[i]->bytes;
+    return n;
+}
+
+namespace rt {
+
+int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
+    *out = nullptr;
+    rt_resident_scene *res = new (std::nothrow) rt_resident_scene();
+    if (!res) {
+        set_error("rt_resident_scene_create: out of host memory");
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    auto fail = [&](int st) {
+        delete res;
+        return st;
+    };
+    cudaGetDevice(&res->device);
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("rt_resident_scene_create: cudaStreamCreate failed");
+        return fail(RT_ERR_CUDA);
+    }
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    } guard{s};
+    int st;
+    // Scene upload (Renderer::new, lib.rs:234-266).
+    if ((st = upload(res->d_tris, sd->triangles, sd->triangle_count, s)) != RT_OK) return fail(st);
+    rt::TraversalLayout lay;
+    if (!rt::build_traversal_layout(sd->bvh_nodes, sd->bvh_node_count, sd->bvh_prims, sd->bvh_prim_count,
+                                    sd->triangles, sd->triangle_count, lay))
+        return fail(RT_ERR_INVALID_ARGUMENT);
+    if ((st = upload(res->d_cnodes, lay.cnodes.data(), lay.cnodes.size(), s)) != RT_OK) return fail(st);
+    if ((st = upload(res->d_tri_ord, lay.tri_ord.data(), lay.tri_ord.size(), s)) != RT_OK) return fail(st);
+    if ((st = upload(res->d_mats, sd->materials, sd->material_count, s)) != RT_OK) return fail(st);
+    res->lights.assign(sd->lights, sd->lights + sd->light_count);
+    rtd::DevScene &ds = res->scene;
+    ds.cnodes = res->d_cnodes.as<float4>();
+    ds.tri_ord = res->d_tri_ord.as<float4>();
+    ds.cnode_count = (uint32_t)(lay.cnodes.size() / 16);
+    // A near-first traversal holds at most one pending entry per tree level.
+    ds.stack_cap = lay.max_depth < 32u ? 32u : 63u;
+    ds.any_hit_shadows = 1u;
+    for (uint64_t i = 0; i < sd->material_count; ++i)
+        if ((sd->materials[i].flags & RT_MAT_FLAG_ALPHA_CUTOUT) && sd->materials[i].tex_albedo != RT_TEX_NONE)
+            ds.any_hit_shadows = 0u;
+    ds.tris = res->d_tris.as<float4>();
+    ds.mats = res->d_mats.as<float4>();
+    ds.tri_count = (uint32_t)sd->triangle_count;
+    ds.mat_count = (uint32_t)sd->material_count;
+    const rt_texture_array *roles[4] = {&sd->tex_albedo, &sd->tex_mr, &sd->tex_emissive, &sd->tex_normal};
+    for (int i = 0; i < 4; ++i) {
+        const rt_texture_array &t = *roles[i];
+        if (t.rgba8 && t.layers && t.width && t.height) {
+            size_t bytes = (size_t)t.width * t.height * t.layers * 4;
+            if ((st = upload(res->d_tex[i], t.rgba8, bytes, s)) != RT_OK) return fail(st);
+            ds.tex[i] = rtd::DevTex{res->d_tex[i].as<uchar4>(), t.width, t.height, t.layers};
+        } else {
+            ds.tex[i] = rtd::DevTex{nullptr, 0, 0, 0};
+        }
+    }
+    // The host copies of the layout are freed when `lay` goes out of scope; wait for the copies first.
+    RT_CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < 3; ++i) {
+        res->bmin[i] = sd->bounds_min[i];
+        res->bmax[i] = sd->bounds_max[i];
+    }
+    res->has_bounds = sd->has_bounds;
+    res->bytes = res->d_cnodes.bytes + res->d_tri_ord.bytes + res->d_tris.bytes + res->d_mats.bytes +
+                 res->d_tex[0].bytes + res->d_tex[1].bytes + res->d_tex[2].bytes + res->d_tex[3].bytes;
+    *out = res;
+    return RT_OK;
+}
+
+void resident_scene_release(rt_resident_scene *s) {
+    if (s && s->refs.fetch_sub(1) == 1u) delete s;
+}
+
+uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
+    return slots * 192u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
+}
+
+uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells) {
+    const uint64_t npix = (uint64_t)c.width * c.height;
+    const uint64_t S = photon_slots_of(c);
+    return npix * (5 * 16 + 4) + S * (64 + 64 + 4 + 4) + num_cells * 16 +
+           (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + sizeof(rtd::DevJob) + 16 + 64 + 64 * 16;
+}
+
+}  // namespace rt
+
+extern "C" int rt_resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
+    rt::clear_error();
+    if (!sd || !out) {
+        set_error("rt_resident_scene_create: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (int st = check_scene_desc(sd, "rt_resident_scene_create")) return st;
+    return rt::resident_scene_create(sd, out);
+}
+
+extern "C" void rt_resident_scene_release(rt_resident_scene *s) { rt::resident_scene_release(s); }
+
+extern "C" uint64_t rt_resident_scene_bytes(const rt_resident_scene *s) { return s ? s->bytes : 0; }
+
+extern "C" uint32_t rt_resident_scene_refs(const rt_resident_scene *s) { return s ? s->refs.load() : 0u; }
+
+extern "C" int rt_renderer_create_resident(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer **out) {
+    rt::clear_error();
+    if (!res || !cfg || !out) {
+        set_error("rt_renderer_create_resident: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (int st = check_config(cfg, "rt_renderer_create_resident")) return st;
+    return create_on(res, cfg, out);
+}
+
+extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_config *cfg, rt_renderer **out) {
+    rt::clear_error();
+    if (!sd || !cfg || !out) {
+        set_error("rt_renderer_create: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (int st = check_config(cfg, "rt_renderer_create")) return st;
+    if (int st = check_scene_desc(sd, "rt_renderer_create")) return st;
+    rt_resident_scene *res = nullptr;
+    if (int st = rt::resident_scene_create(sd, &res)) return st;
+    const int st = create_on(res, cfg, out);
+    rt::resident_scene_release(res);  // the renderer holds its own reference
+    return st;
+}
+
+extern "C" uint64_t rt_renderer_device_bytes(const rt_renderer *r) { return r ? r->device_bytes() : 0; }
+
+extern "C" int rt_renderer_footprint(const rt_render_config *cfg, const rt_resident_scene *res, uint64_t *create_bytes,
+                                     uint64_t *solo_path_bytes) {
+    rt::clear_error();
+    if (!cfg || !res || !create_bytes) {
+        set_error("rt_renderer_footprint: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    if (int st = check_config(cfg, "rt_renderer_footprint")) return st;
+    rt_grid_params gp;
+    float radius = cfg->photon_radius;
+    rt_derive_grid(res->bmin, res->bmax, (int)res->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
+                   (uint32_t)photon_slots_of(*cfg), &gp, &radius);
+    *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells);
+    if (solo_path_bytes) {
+        const uint32_t spp = cfg->spp > 1u ? cfg->spp : 1u;
+        *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg));
+    }
+    return RT_OK;
+}
+
 extern "C" void rt_renderer_destroy(rt_renderer *r) { delete r; }
 
-extern "C" int rt_render_frame(rt_renderer *r) {
-    if (int st = check_renderer(r, "rt_render_frame")) return st;
-    rt::clear_error();
-    cudaStream_t s = r->stream;
+namespace rt {
+
+float prepare_frame(rt_renderer *r) {
     const rt_render_config &c = r->cfg;
     // lib.rs:672-684
     r->sample_counter += 1u;
     if (r->frames_since_reset != 0xFFFFFFFFu) r->frames_since_reset += 1u;
-    const float alpha =
-        c.accumulate_frames == 0 ? 1.0f : 1.0f / (float)std::min(r->frames_since_reset, c.accumulate_frames);
-    const size_t npix = (size_t)c.width * c.height;
+    return c.accumulate_frames == 0 ? 1.0f : 1.0f / (float)std::min(r->frames_since_reset, c.accumulate_frames);
+}
 
-    cudaEvent_t fe[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (auto &e : fe) RT_CK(r->ring.next(&e));
-    RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
-    const uint32_t spp = c.spp > 1u ? c.spp : 1u;
-    const uint32_t iters = spp * max_bounces(c);
-    const size_t counts_bytes = sizeof(uint32_t) * 4 * ((size_t)iters + 1);
-    if (counts_bytes > r->w_counts_bytes) {
-        RT_CK(cudaStreamSynchronize(s));
-        RT_CK(r->w_counts.alloc(counts_bytes));
-        r->w_counts_bytes = counts_bytes;
-    }
-    rtd::WaveParams wp;
-    std::memset(&wp, 0, sizeof(wp));
-    wp.scene = r->scene;
-    wp.cam = r->cam;
-    wp.ip = image_params(r, alpha);
-    wp.gp = r->gp;
-    wp.sorted_photons = r->d_sorted.as<float4>();
-    wp.sorted_count = r->photon_slots;
-    wp.grid_meta = r->d_meta.as<uint2>();
-    wp.max_bounces = max_bounces(c);
-    wp.npix = (uint32_t)npix;
-    wp.ro = r->w_ro.as<float4>();
-    wp.rd = r->w_rd.as<float4>();
-    wp.thr = r->w_thr.as<float4>();
-    wp.hit = r->w_hit.as<float2>();
-    wp.acc = r->w_acc.as<float4>();
-    wp.nrm = r->w_nrm.as<float4>();
-    wp.queue[0] = r->w_queue[0].as<uint32_t>();
-    wp.queue[1] = r->w_queue[1].as<uint32_t>();
-    wp.counts = r->w_counts.as<uint32_t>();
-    wp.shadow = r->w_shadow.as<float4>();
-    wp.frame = r->d_frame.as<float4>();
-    wp.moments = r->d_moments.as<float4>();
-    wp.gbuffer = r->d_gbuffer.as<float4>();
-    wp.counters = r->d_counters.as<unsigned long long>();
-    RT_CK(rtd::launch_wavefront(wp, iters, r->num_sms, s));
-    RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
+uint32_t frame_iterations(const rt_renderer *r) {
+    const uint32_t spp = r->cfg.spp > 1u ? r->cfg.spp : 1u;
+    return spp * max_bounces(r->cfg);
+}
 
+rtd::DevJob make_job(const rt_renderer *r, uint32_t base) {
+    const rt_render_config &c = r->cfg;
+    rtd::DevJob j;
+    std::memset(&j, 0, sizeof(j));
+    j.scene = r->scene;
+    j.cam = r->cam;
+    j.ip = image_params(r, c.accumulate_frames == 0 ? 1.0f
+                                                    : 1.0f / (float)std::min(r->frames_since_reset, c.accumulate_frames));
+    j.gp = r->gp;
+    j.sorted_photons = r->d_sorted.as<float4>();
+    j.sorted_count = r->photon_slots;
+    j.grid_meta = r->d_meta.as<uint2>();
+    j.max_bounces = max_bounces(c);
+    j.npix = c.width * c.height;
+    j.base = base;
+    j.spp = c.spp > 1u ? c.spp : 1u;
+    j.frame = r->d_frame.as<float4>();
+    j.moments = r->d_moments.as<float4>();
+    j.gbuffer = r->d_gbuffer.as<float4>();
+    j.alpha = j.ip.accumulate_alpha;
+    return j;
+}
+
+int enqueue_denoise(rt_renderer *r, float alpha, const float *alpha_dev, cudaStream_t s, float4 **result_out) {
+    const rt_render_config &c = r->cfg;
     // lib.rs:743-776: a-trous passes, steps 1, 2, ..., ping-pong frame <-> pingpong.
     float4 *result = r->d_frame.as<float4>();
-    uint32_t passes = c.enable_denoise ? denoise_passes(c) : 0u;
+    const uint32_t passes = c.enable_denoise ? denoise_passes(c) : 0u;
     for (uint32_t it = 0; it < passes; ++it) {
         rt_denoise_params dp;
         std::memset(&dp, 0, sizeof(dp));
@@ -443,13 +470,16 @@ extern "C" int rt_render_frame(rt_renderer *r) {
         dp.alpha = alpha;
         const float4 *in = (it % 2 == 0) ? r->d_frame.as<float4>() : r->d_pingpong.as<float4>();
         float4 *o = (it % 2 == 0) ? r->d_pingpong.as<float4>() : r->d_frame.as<float4>();
-        RT_CK(rtd::launch_denoise(in, o, r->d_gbuffer.as<float4>(), r->d_moments.as<float4>(), dp, s));
+        RT_CK(rtd::launch_denoise(in, o, r->d_gbuffer.as<float4>(), r->d_moments.as<float4>(), dp, alpha_dev, s));
         result = o;
     }
     r->last_denoise_passes = passes;
-    RT_CK(cudaEventRecord(r->events.ev[EV_DENOISE1], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[2], s));
+    *result_out = result;
+    return RT_OK;
+}
 
+int enqueue_resolve(rt_renderer *r, const float4 *result, float alpha, const float *alpha_dev, cudaStream_t s) {
+    const rt_render_config &c = r->cfg;
     // lib.rs:778-831: composite, then tonemap.
     rt_tonemap_params tp;
     std::memset(&tp, 0, sizeof(tp));
@@ -458,11 +488,49 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     tp.width = c.width;
     tp.glow = r->glow;
     std::memcpy(tp.marker, r->marker, sizeof(tp.marker));
-    RT_CK(rtd::launch_resolve(result, r->d_accum.as<float4>(), r->d_gbuffer.as<float4>(), c.width, c.height, alpha, tp,
-                              r->d_output.as<uchar4>(), s));
+    RT_CK(rtd::launch_resolve(result, r->d_accum.as<float4>(), r->d_gbuffer.as<float4>(), c.width, c.height, alpha,
+                              alpha_dev, tp, r->d_output.as<uchar4>(), s));
+    return RT_OK;
+}
+
+int enqueue_post(rt_renderer *r, float alpha, const float *alpha_dev, cudaStream_t s) {
+    float4 *result = nullptr;
+    if (int st = enqueue_denoise(r, alpha, alpha_dev, s, &result)) return st;
+    return enqueue_resolve(r, result, alpha, alpha_dev, s);
+}
+
+}  // namespace rt
+
+extern "C" int rt_render_frame(rt_renderer *r) {
+    if (int st = check_renderer(r, "rt_render_frame")) return st;
+    rt::clear_error();
+    cudaStream_t s = r->stream;
+    const rt_render_config &c = r->cfg;
+    const float alpha = rt::prepare_frame(r);
+    const uint32_t iters = rt::frame_iterations(r);
+    const size_t npix = (size_t)c.width * c.height;
+    if (npix > r->path.slots || sizeof(uint32_t) * 4 * ((size_t)iters + 1) > r->path.counts_bytes) {
+        RT_CK(cudaStreamSynchronize(s));
+        RT_CK(r->path.ensure(npix, iters));
+    }
+    cudaEvent_t fe[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (auto &e : fe) RT_CK(r->ring.next(&e));
+    RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
+    if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
+    const rtd::DevJob job = rt::make_job(r, 0u);
+    RT_CK(r->jobs.upload(&job, 1, s));
+    const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
+    const rtd::JobShape shape{c.width, c.height, (uint32_t)npix, 0u, r->scene.stack_cap};
+    RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, s));
+    RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
+    if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
+    float4 *result = nullptr;
+    if (int st = rt::enqueue_denoise(r, alpha, nullptr, s, &result)) return st;
+    RT_CK(cudaEventRecord(r->events.ev[EV_DENOISE1], s));
+    if (fe[3]) RT_CK(cudaEventRecord(fe[2], s));
+    if (int st = rt::enqueue_resolve(r, result, alpha, nullptr, s)) return st;
     RT_CK(cudaEventRecord(r->events.ev[EV_RESOLVE1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[3], s));
-    (void)npix;
     r->frames += 1;
     r->have_frame_timing = true;
     return RT_OK;
@@ -538,8 +606,7 @@ static int build_grid(rt_renderer *r) {
     return RT_OK;
 }
 
-extern "C" int rt_rebuild_photons(rt_renderer *r) {
-    if (int st = check_renderer(r, "rt_rebuild_photons")) return st;
+int rt::enqueue_photon_rebuild(rt_renderer *r) {
     if (!r->photon_buffers) {
         set_error("rt_rebuild_photons: the renderer was created with enable_photon_map = 0 (no photon buffers)");
         return RT_ERR_STATE;
@@ -563,8 +630,14 @@ extern "C" int rt_rebuild_photons(rt_renderer *r) {
     RT_CK(cudaEventRecord(r->events.ev[EV_TRACE1], s));
     if (int st = build_grid(r)) return st;
     RT_CK(cudaEventRecord(r->events.ev[EV_GRID1], s));
-    RT_CK(cudaStreamSynchronize(s));
     r->have_photon_timing = true;
+    return RT_OK;
+}
+
+extern "C" int rt_rebuild_photons(rt_renderer *r) {
+    if (int st = check_renderer(r, "rt_rebuild_photons")) return st;
+    if (int st = rt::enqueue_photon_rebuild(r)) return st;
+    RT_CK(cudaStreamSynchronize(r->stream));
     return RT_OK;
 }
 
@@ -781,7 +854,7 @@ extern "C" int rt_stage_denoise(const float *frame_rgba, const float *gbuffer, c
         dp.phi_normal = 12.0f;
         dp.phi_depth = 0.05f;
         dp.alpha = alpha;
-        RT_CK(rtd::launch_denoise(cur, nxt, g.as<float4>(), m.as<float4>(), dp, 0));
+        RT_CK(rtd::launch_denoise(cur, nxt, g.as<float4>(), m.as<float4>(), dp, nullptr, 0));
         std::swap(cur, nxt);
     }
     RT_CK(cudaMemcpy(out_rgba, cur, bytes, cudaMemcpyDeviceToHost));
@@ -810,7 +883,7 @@ extern "C" int rt_stage_resolve(const float *frame_rgba, float *accum_inout, con
     }
     rt_tonemap_params t = *tp;
     t.width = width;
-    RT_CK(rtd::launch_resolve(f.as<float4>(), a.as<float4>(), gp, width, height, alpha, t, o.as<uchar4>(), 0));
+    RT_CK(rtd::launch_resolve(f.as<float4>(), a.as<float4>(), gp, width, height, alpha, nullptr, t, o.as<uchar4>(), 0));
     RT_CK(cudaMemcpy(accum_inout, a.p, bytes, cudaMemcpyDeviceToHost));
     RT_CK(cudaMemcpy(out_rgba8, o.p, bytes / 4, cudaMemcpyDeviceToHost));
     return RT_OK;

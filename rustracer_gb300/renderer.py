@@ -69,14 +69,59 @@ class RenderConfig:
         return RenderConfig(**kw)
 
 
-class Renderer:
-    """Renderer (lib.rs:189-1042): owns every device buffer; not thread-safe."""
+class ResidentScene:
+    """A scene uploaded once and shared by every renderer created on it (rt_resident_scene_*)."""
 
-    def __init__(self, scene: Scene | A.SceneDesc, config: RenderConfig):
+    def __init__(self, scene: Scene | A.SceneDesc):
         self._lib = A.load()
         desc = scene.describe() if isinstance(scene, Scene) else scene
         h = C.c_void_p()
-        A.check("rt_renderer_create", self._lib.rt_renderer_create(C.byref(desc), C.byref(config.to_c()), C.byref(h)))
+        A.check("rt_resident_scene_create", self._lib.rt_resident_scene_create(C.byref(desc), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def device_bytes(self) -> int:
+        return int(self._lib.rt_resident_scene_bytes(self._h))
+
+    def refs(self) -> int:
+        return int(self._lib.rt_resident_scene_refs(self._h))
+
+    def footprint(self, config: RenderConfig) -> tuple[int, int]:
+        """(bytes a renderer with `config` allocates at create, path bytes its first solo frame adds)."""
+        a, b = C.c_uint64(), C.c_uint64()
+        A.check("rt_renderer_footprint", self._lib.rt_renderer_footprint(C.byref(config.to_c()), self._h,
+                                                                         C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.rt_resident_scene_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Renderer:
+    """Renderer (lib.rs:189-1042): owns every device buffer; not thread-safe.  `scene` is a Scene (or
+    its description), uploaded for this renderer, or a ResidentScene shared with other renderers."""
+
+    def __init__(self, scene: Scene | A.SceneDesc | ResidentScene, config: RenderConfig):
+        self._lib = A.load()
+        h = C.c_void_p()
+        if isinstance(scene, ResidentScene):
+            A.check("rt_renderer_create_resident",
+                    self._lib.rt_renderer_create_resident(scene.handle, C.byref(config.to_c()), C.byref(h)))
+        else:
+            desc = scene.describe() if isinstance(scene, Scene) else scene
+            A.check("rt_renderer_create",
+                    self._lib.rt_renderer_create(C.byref(desc), C.byref(config.to_c()), C.byref(h)))
         self._h = h
         self._scene = scene  # keeps the borrowed arrays alive for the renderer's lifetime
 
@@ -176,6 +221,9 @@ class Renderer:
     def stream(self) -> int:
         return int(self._lib.rt_renderer_stream(self._h) or 0)
 
+    def device_bytes(self) -> int:
+        return int(self._lib.rt_renderer_device_bytes(self._h))
+
     # ---- read-backs ------------------------------------------------------------------------------
     def _img(self, fn: str) -> np.ndarray:
         c = self.config
@@ -221,6 +269,47 @@ class Renderer:
         meta = np.empty((n, 2), np.uint32)
         A.check("rt_read_photon_grid", self._lib.rt_read_photon_grid(self._h, A.ptr(counts), A.ptr(meta), n))
         return counts, meta
+
+
+class Batch:
+    """Renders the next frame of several renderers at once (rt_batch_*); their rays share the same
+    wavefront launches.  use_graphs captures each batch frame as a CUDA graph."""
+
+    def __init__(self, renderers: list[Renderer], use_graphs: bool = True):
+        self._lib = A.load()
+        self.renderers = list(renderers)  # kept alive for the batch's lifetime
+        arr = (C.c_void_p * len(renderers))(*[r.handle.value for r in renderers])
+        h = C.c_void_p()
+        A.check("rt_batch_create", self._lib.rt_batch_create(arr, len(renderers), int(use_graphs), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.rt_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render_frame(self) -> None:
+        A.check("rt_batch_render_frame", self._lib.rt_batch_render_frame(self._h))
+
+    def render_frames(self, n: int) -> None:
+        A.check("rt_batch_render_frames", self._lib.rt_batch_render_frames(self._h, n))
+
+    def synchronize(self) -> None:
+        A.check("rt_batch_synchronize", self._lib.rt_batch_synchronize(self._h))
+
+    def stats(self) -> A.FrameStats:
+        s = A.FrameStats()
+        A.check("rt_batch_get_stats", self._lib.rt_batch_get_stats(self._h, C.byref(s)))
+        return s
+
+    def stream(self) -> int:
+        return int(self._lib.rt_batch_stream(self._h) or 0)
 
 
 def render_config_default() -> RenderConfig:
