@@ -338,11 +338,15 @@ uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
     return slots * 192u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
 }
 
-uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells) {
+uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {
+    // The allocations of create_on: frame buffers (5 x float4 + rgba8 per pixel), photon slots, keys,
+    // slot order and sorted photons, counts / cursor / meta per cell, scan partials, grid totals,
+    // counters, the one-entry job table and the renderer's own light buffer.
     const uint64_t npix = (uint64_t)c.width * c.height;
     const uint64_t S = photon_slots_of(c);
     return npix * (5 * 16 + 4) + S * (64 + 64 + 4 + 4) + num_cells * 16 +
-           (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + sizeof(rtd::DevJob) + 16 + 64 + 64 * 16;
+           (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + 16 + 64 + sizeof(rtd::DevJob) +
+           sizeof(rt_light) * std::max<uint64_t>(n_lights, 1);
 }
 
 }  // namespace rt
@@ -405,7 +409,7 @@ extern "C" int rt_renderer_footprint(const rt_render_config *cfg, const rt_resid
     float radius = cfg->photon_radius;
     rt_derive_grid(res->bmin, res->bmax, (int)res->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
                    (uint32_t)photon_slots_of(*cfg), &gp, &radius);
-    *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells);
+    *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells, res->lights.size());
     if (solo_path_bytes) {
         const uint32_t spp = cfg->spp > 1u ? cfg->spp : 1u;
         *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg));

@@ -224,7 +224,7 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out);
 void resident_scene_release(rt_resident_scene *s);
 // Device bytes a renderer with this config allocates at create (frame and photon buffers), and the
 // path state its first solo frame adds.
-uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells);
+uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights);
 uint64_t path_state_bytes(uint64_t slots, uint32_t iters);
 // rebuild_photons (lib.rs:913-1037) enqueued on the renderer's stream, without waiting for it.
 int enqueue_photon_rebuild(rt_renderer *r);
