@@ -161,31 +161,39 @@ def cpu_sample(scene, cfg, cam, seconds: float, threads: int, frames: int = 1):
     _gather_rows(o, (cfg.height // 2 - rows // 2, cfg.height // 2 - rows // 2 + rows))
     dt = time.perf_counter() - t0
     per_row = dt / rows
-    band = int(max(1, min(cfg.height, seconds / max(per_row, 1e-6) / max(frames, 1))))
-    y0 = max(0, cfg.height // 2 - band // 2)
+    rows_total = int(max(1, min(cfg.height, seconds / max(per_row, 1e-6) / max(frames, 1))))
+    # eight bands spread evenly over the frame, so that the per-ray work counts are the frame's
+    n_bands = min(8, rows_total)
+    band = max(1, rows_total // n_bands)
+    starts = [int(round((i + 0.5) * cfg.height / n_bands - band / 2)) for i in range(n_bands)]
+    starts = [min(max(0, y), cfg.height - band) for y in starts]
     o.counters[:] = 0
     t0 = time.perf_counter()
     for f in range(frames):
-        _gather_rows(o, (y0, y0 + band))
+        for i, y in enumerate(starts):
+            _gather_rows(o, (y, y + band), new_frame=i == 0)
     dt = time.perf_counter() - t0
     c = o.counters.astype(np.float64)
     seg = c[0]
-    desc = (f"rows {y0}..{y0 + band} of {frames} frame(s) of {cfg.width}x{cfg.height}, spp {cfg.spp}, "
-            f"depth {cfg.max_bounces or 6} ({int(seg)} segments in {dt:.1f} s)")
+    desc = (f"{n_bands} bands of {band} rows ({n_bands * band} of {cfg.height}) of {frames} frame(s) of "
+            f"{cfg.width}x{cfg.height}, spp {cfg.spp}, depth {cfg.max_bounces or 6} ({int(seg)} segments in "
+            f"{dt:.1f} s)")
     rays = max(c[0] + c[1], 1.0)
     work = {"nodes_per_ray": c[2] / rays, "tris_per_ray": c[3] / rays, "hit_fraction": c[4] / max(c[0], 1.0),
             "shadow_per_segment": c[1] / max(c[0], 1.0)}
     return seg / dt, desc, work
 
 
-def _gather_rows(o, rows):
-    """One gather dispatch of the oracle over a row band (the CPU cost of the frame)."""
+def _gather_rows(o, rows, new_frame: bool = True):
+    """One gather dispatch of the oracle over a row band (the CPU cost of the frame); new_frame
+    advances the frame counter first."""
     import ctypes as C
 
     import oracle
 
-    o.sample_counter += 1
-    o.frames_since_reset += 1
+    if new_frame:
+        o.sample_counter += 1
+        o.frames_since_reset += 1
     ip = o.image_params(o.alpha())
     mb = o.cfg.max_bounces or 6
     oracle.load().oracle_gather(C.cast(C.pointer(o.desc), C.c_void_p), C.byref(o.cam), C.byref(ip), mb,
@@ -369,9 +377,11 @@ def frame_launches(cfgs) -> int:
 
 
 def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> dict:
-    """64 jobs rendered (a) one job at a time with its own per-frame launches and (b) as one batch per
-    progressive frame captured as a CUDA graph.  Both render warmup + steps frames of every job from
-    a fresh renderer; the final accumulations are compared bit for bit (equal per-job RMSE)."""
+    """64 jobs rendered (a) one job at a time with its own per-frame launches (default launch shape)
+    and (b) as one batch per progressive frame captured as a CUDA graph, `steps` frames with the
+    default launch shape, then the autotuner, then `steps` frames with the tuned shape.  Both arms
+    render warmup + 2 steps frames of every job from a fresh renderer; the final accumulations are
+    compared bit for bit (equal per-job RMSE)."""
     import hashlib
 
     import torch
@@ -400,7 +410,7 @@ def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> di
         r.synchronize()
         s0 = r.stats()
         t0 = time.perf_counter()
-        r.render_frames(steps)
+        r.render_frames(2 * steps)
         r.synchronize()
         plain_s += time.perf_counter() - t0
         plain_seg += r.stats().segments - s0.segments
@@ -412,18 +422,26 @@ def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> di
     b = rt.Batch(rs, use_graphs=True)
     b.render_frames(warmup)
     b.synchronize()
-    s0 = b.stats()
     stream = torch.cuda.ExternalStream(b.stream())
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    ev0.record(stream)
-    b.render_frames(steps)
-    ev1.record(stream)
-    b.synchronize()
-    batch_s = time.perf_counter() - t0
-    batch_dev_ms = ev0.elapsed_time(ev1)
+
+    def timed():
+        s0 = b.stats()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        b.render_frames(steps)
+        ev1.record(stream)
+        b.synchronize()
+        wall = time.perf_counter() - t0
+        return b.stats().segments - s0.segments, wall, ev0.elapsed_time(ev1)
+
+    default_shape = b.tuning
+    seg_d, wall_d, _ = timed()
+    t_tune = time.perf_counter()
+    tuned_shape, tuned_ms = b.autotune(trial_frames=1)
+    tune_s = time.perf_counter() - t_tune
+    batch_seg, batch_s, batch_dev_ms = timed()
     s1 = b.stats()
-    batch_seg = s1.segments - s0.segments
     same = all(digest(r) == h for r, h in zip(rs, plain_hash))
     b.close()
     for r in rs:
@@ -438,9 +456,12 @@ def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> di
         "plain_segments_per_s": plain_v,
         "batched_segments_per_s": batch_v,
         "batched_device_segments_per_s": batch_seg / (batch_dev_ms / 1000.0),
+        "batched_default_shape_segments_per_s": seg_d / wall_d,
         "speedup": batch_v / plain_v,
         "segments_per_frame": batch_seg / steps,
-        "identical_outputs": bool(same and plain_seg == batch_seg),
+        "identical_outputs": bool(same and plain_seg == seg_d + batch_seg),
+        "autotune": {"default": default_shape, "chosen": tuned_shape, "ms_per_frame": tuned_ms,
+                     "seconds": tune_s},
         "graph_captures": int(s1.graph_captures),
         "gpu_launches_per_frame": frame_launches([job_objects(s, pool)[1] for s in specs]),
         "resident_scenes": len(resident),
@@ -462,10 +483,11 @@ def served_trace(rate: float, seconds: float, pool, seed: int) -> list[tuple[flo
         out.append((t, spec, budget))
 
 
-def served_arm(mode: str, trace, pool, seconds: float) -> dict:
+def served_arm(mode: str, trace, pool, seconds: float, tuning: dict | None) -> dict:
     import rustracer_gb300 as rt
 
-    srv = rt.Server(mode=mode, graphs=True, hbm_cap_bytes=120 << 30, max_jobs=64, max_slots=1 << 25)
+    srv = rt.Server(mode=mode, graphs=True, hbm_cap_bytes=120 << 30, max_jobs=64, max_slots=1 << 25,
+                    tuning=tuning)
     for i, (_, sc) in enumerate(pool):
         srv.add_scene(i, sc)
     ids = []
@@ -498,13 +520,13 @@ def served_arm(mode: str, trace, pool, seconds: float) -> dict:
     }
 
 
-def served_leg(rate: float, seconds: float, pool, seed: int = 5) -> dict:
+def served_leg(rate: float, seconds: float, pool, tuning: dict | None, seed: int = 5) -> dict:
     """The request loop under Poisson arrivals, continuous batching against the one-job-at-a-time
     loop on the same arrival trace.  Percentiles are over the jobs that reached their first frame /
     their budget inside the window (the rest are still queued when it closes)."""
     trace = served_trace(rate, seconds, pool, seed)
-    batched = served_arm("batched", trace, pool, seconds)
-    plain = served_arm("plain", trace, pool, seconds)
+    batched = served_arm("batched", trace, pool, seconds, tuning)
+    plain = served_arm("plain", trace, pool, seconds, None)
     return {
         "workload": f"Poisson arrivals at {rate} jobs/s for {seconds} s over a pool of {len(pool)} scenes "
                     f"(10k-2M triangles), budgets log-uniform in [8, 256] frames, HBM cap 120 GiB",
@@ -619,7 +641,8 @@ def run_ours(args, w):
         stages = photon_denoise_stages(args.steps, args.warmup, peak) if args.stages else None
         pool = scene_pool(32, 7) if (args.batched or args.served) else None
         batched = batched_leg(args.batched_jobs, args.batched_steps, 2, pool) if args.batched else None
-        served = served_leg(args.served_rate, args.served_seconds, pool) if args.served else None
+        shape = batched["autotune"]["chosen"] if batched else None
+        served = served_leg(args.served_rate, args.served_seconds, pool, shape) if args.served else None
         line = {
             "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,

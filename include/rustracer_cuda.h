@@ -356,6 +356,16 @@ int rt_load_photons_and_build_grid(rt_renderer *r, const rt_photon *photons, uin
  * and captured again only when the launches' shape or baked settings change.
  * ------------------------------------------------------------------------------------------- */
 typedef struct rt_batch rt_batch;
+/* Launch shape of the persistent traversal kernels (closest-hit and shadow rays).  It changes only
+ * speed, never a result.  Fields outside the supported set are clamped: block_threads 64 / 128 /
+ * 256, blocks_per_sm up to 2048 / block_threads, chunk (queue items a warp takes per atomic, its
+ * segment of the shared queue) 32 .. 1024 in steps of 32, steps (traversal records between lane
+ * refills) 1 .. 64, stack_entries 32 / 48 / 64 per lane, raised to what the jobs' trees need.
+ * Default: 128 threads, 8 blocks per SM, chunk 64, 8 steps, 32 entries. */
+typedef struct rt_wavefront_tuning {
+    uint32_t block_threads, blocks_per_sm, chunk, steps, stack_entries;
+    uint32_t _pad[3];
+} rt_wavefront_tuning;
 int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out);
 void rt_batch_destroy(rt_batch *b);
 int rt_batch_render_frame(rt_batch *b);
@@ -365,6 +375,17 @@ int rt_batch_synchronize(rt_batch *b);
  * timed_frames cover the batch frames since the previous call. */
 int rt_batch_get_stats(rt_batch *b, rt_frame_stats *out);
 void *rt_batch_stream(rt_batch *b);
+int rt_batch_set_tuning(rt_batch *b, const rt_wavefront_tuning *t);
+int rt_batch_get_tuning(rt_batch *b, rt_wavefront_tuning *t);
+/* The autotuner: renders trial frames of the batch under candidate launch shapes (coordinate
+ * descent over block shape, blocks per SM, stack depth, chunk size and refill steps; trial_frames
+ * frames per candidate, timed with CUDA events) and keeps the fastest.  The trial frames are undone
+ * -- every job's image buffers and frame counters are restored -- so the frames rendered afterwards
+ * are the ones that would have been rendered without tuning.  best / best_ms may be null. */
+int rt_batch_autotune(rt_batch *b, uint32_t trial_frames, rt_wavefront_tuning *best, float *best_ms);
+/* The same launch shape for a renderer's own frames (rt_render_frame). */
+int rt_set_tuning(rt_renderer *r, const rt_wavefront_tuning *t);
+int rt_get_tuning(const rt_renderer *r, rt_wavefront_tuning *t);
 
 /* ---------------------------------------------------------------------------------------------
  * The render-request loop (no counterpart in the reference, which renders one job per process):
@@ -400,6 +421,7 @@ typedef struct rt_server_config {
     uint32_t graphs;            /* batched mode: capture a batch frame whose shape repeats        */
     uint32_t frames_in_flight;  /* frames queued on the GPU ahead of the host, 0: 2               */
     uint32_t _pad;
+    rt_wavefront_tuning tuning; /* launch shape of the batch frames; all zero: the default        */
 } rt_server_config;
 typedef struct rt_request {
     uint32_t scene_id;          /* as registered with rt_server_add_scene                         */
@@ -464,7 +486,8 @@ int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_params *gp, uin
  * with a no-allocation rule (cudaMalloc / cudaFree can synchronise the device), hosts whose device
  * memory all comes from their own allocator or pool, and processes near the memory limit.
  *   - d_photons (gp->photon_slots records), d_counts (gp->num_cells), d_meta (2 * gp->num_cells) and
- *     d_sorted (gp->photon_slots records) are DEVICE pointers owned by the caller; entries of d_sorted
+ *     d_sorted (gp->photon_slots records) are DEVICE pointers owned by the caller (photon buffers
+ *     16-byte aligned, counts / meta 4-byte aligned, as cudaMalloc returns them); entries of d_sorted
  *     past the number of binned photons are left as they were.
  *   - Scratch lives in one file-scope device array of RT_NOALLOC_SCRATCH_BYTES that every GPU loading
  *     the library holds until the process exits; sizes above RT_NOALLOC_MAX_SLOTS slots or

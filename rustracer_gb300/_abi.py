@@ -144,9 +144,17 @@ SERVER_BATCHED, SERVER_PLAIN = 0, 1
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 
+class WavefrontTuning(C.Structure):
+    _fields_ = [("block_threads", u32), ("blocks_per_sm", u32), ("chunk", u32), ("steps", u32),
+                ("stack_entries", u32), ("_pad", u32 * 3)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_ if f != "_pad"}
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_cap_bytes", C.c_uint64), ("max_jobs", u32), ("max_slots", u32), ("mode", u32),
-                ("graphs", u32), ("frames_in_flight", u32), ("_pad", u32)]
+                ("graphs", u32), ("frames_in_flight", u32), ("_pad", u32), ("tuning", WavefrontTuning)]
 
 
 class Request(C.Structure):
@@ -219,6 +227,11 @@ _PROTOS: dict[str, tuple] = {
     "rt_batch_synchronize": (C.c_int, [vp]),
     "rt_batch_get_stats": (C.c_int, [vp, P(FrameStats)]),
     "rt_batch_stream": (vp, [vp]),
+    "rt_batch_set_tuning": (C.c_int, [vp, P(WavefrontTuning)]),
+    "rt_batch_get_tuning": (C.c_int, [vp, P(WavefrontTuning)]),
+    "rt_batch_autotune": (C.c_int, [vp, u32, P(WavefrontTuning), P(C.c_float)]),
+    "rt_set_tuning": (C.c_int, [vp, P(WavefrontTuning)]),
+    "rt_get_tuning": (C.c_int, [vp, P(WavefrontTuning)]),
     "rt_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
     "rt_server_destroy": (None, [vp]),
     "rt_server_add_scene": (C.c_int, [vp, u32, P(SceneDesc)]),

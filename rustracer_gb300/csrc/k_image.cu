@@ -76,30 +76,41 @@ __global__ void __launch_bounds__(256) denoise_kernel(const float4 *__restrict__
 // column, (x, y + k*step) for k = 0..3, whose 5 x 5 tap windows share four of their five rows, so a
 // tap row is read from shared memory once for up to four pixels (40 reads for 4 pixels instead of
 // 100); a warp's lanes read consecutive x (no bank conflicts).  Tiles entirely inside the image skip
-// the bounds tests.  Weights are evaluated as
-//   sw * pow(n.n', phi_n) * exp(-(|dc - dn| / (phi_d max(dc, 1e-4)) + dl^2 / (lambda var + 1e-6))),
-// the reference's product with the two exponentials merged and pow(x, 12) taken by squaring; this
-// file is compiled with FMA contraction.  Results differ from the separate expf / powf form by a few
-// ulps of the weights.
+// the bounds tests.  A tap's weight is evaluated as
+//   pow(max(n.n', 0), 12) * 2^(log2(B3(dx) B3(dy)) - log2(e) |dc - dn| / (phi_d max(dc, 1e-4))
+//                                                  - log2(e) dl^2 / (lambda var + 1e-6)),
+// the reference's product sw * nw * exp(depth term) * exp(luminance term) with the two exponentials
+// and the spline weight merged into one base-2 exponential (ex2.approx), pow(x, 12) taken by
+// squaring; this file is compiled with FMA contraction.  Results differ from the separate expf /
+// powf form by a few ulps of the weights.
 constexpr int kDnBX = 32, kDnRows = 32, kDnThreadsY = 8, kDnPix = 4;
+constexpr float kLog2e = 1.4426950408889634f;
+// log2 of the B3-spline taps 3/8, 1/4, 1/16 (index |offset|)
+__device__ __forceinline__ constexpr float log_b3(int a) {
+    return a == 0 ? -1.4150374992788438f : (a == 1 ? -2.0f : -4.0f);
+}
 
-template <int kStep, bool kInterior>
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+template <int kStep, bool kInterior, bool kPow12>
 __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * kStep],
                                                const float4 (*s_nd)[kDnBX + 4 * kStep], const float *s_varc,
                                                int lx, int ly0, int x, int y0, int W, int Hh, const rt_denoise_params &p,
                                                float4 *__restrict__ out) {
     constexpr int H = 2 * kStep;
-    const float k1d[3] = {0.375f, 0.25f, 0.0625f};
-    const bool pow12 = p.phi_normal == 12.0f;
     float4 cc[kDnPix], cn[kDnPix];
-    float inv_dc[kDnPix], inv_dd[kDnPix];
+    float a_l[kDnPix], a_d[kDnPix];
     float sr[kDnPix], sg[kDnPix], sb[kDnPix], tot[kDnPix];
 #pragma unroll
     for (int k = 0; k < kDnPix; ++k) {
         cc[k] = s_cl[ly0 + H + k * kStep][lx + H];
         cn[k] = s_nd[ly0 + H + k * kStep][lx + H];
-        inv_dc[k] = 1.0f / (s_varc[k] * p.lambda + 1e-6f);
-        inv_dd[k] = 1.0f / (p.phi_depth * fmaxf(cn[k].w, 1e-4f));
+        a_l[k] = -kLog2e * __frcp_rn(s_varc[k] * p.lambda + 1e-6f);
+        a_d[k] = -kLog2e * __frcp_rn(p.phi_depth * fmaxf(cn[k].w, 1e-4f));
         sr[k] = sg[k] = sb[k] = tot[k] = 0.0f;
     }
     // Tap rows j = 0 .. 7 (row offset (j - 2) * step from the first pixel); pixel k uses rows k .. k+4.
@@ -122,18 +133,20 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
                 }
                 const float d = fmaxf(cn[k].x * nd.x + cn[k].y * nd.y + cn[k].z * nd.z, 0.0f);
                 float nw;
-                if (pow12) {
+                if (kPow12) {
                     const float d2 = d * d, d4 = d2 * d2, d8 = d4 * d4;
                     nw = d8 * d4;
                 } else {
                     nw = powf(d, p.phi_normal);
                 }
                 const float dl = nb.w - cc[k].w;
-                const float e = __expf(-(fabsf(cn[k].w - nd.w) * inv_dd[k] + dl * dl * inv_dc[k]));
-                const float w = (k1d[dx < 0 ? -dx : dx] * k1d[dy < 0 ? -dy : dy]) * nw * e;
-                sr[k] += nb.x * w;
-                sg[k] += nb.y * w;
-                sb[k] += nb.z * w;
+                const float lsw = log_b3(dx < 0 ? -dx : dx) + log_b3(dy < 0 ? -dy : dy);
+                float t = fmaf(fabsf(cn[k].w - nd.w), a_d[k], lsw);
+                t = fmaf(dl * a_l[k], dl, t);
+                const float w = nw * ex2_approx(t);
+                sr[k] = fmaf(nb.x, w, sr[k]);
+                sg[k] = fmaf(nb.y, w, sg[k]);
+                sb[k] = fmaf(nb.z, w, sb[k]);
                 tot[k] += w;
             }
         }
@@ -143,13 +156,17 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
         const int y = y0 + k * kStep;
         if (!kInterior && (x >= W || y >= Hh)) continue;
         const size_t idx = (size_t)y * W + x;
-        if (tot[k] > 1e-6f) out[idx] = make_float4(sr[k] / tot[k], sg[k] / tot[k], sb[k] / tot[k], 1.0f);
-        else out[idx] = make_float4(cc[k].x, cc[k].y, cc[k].z, 1.0f);
+        if (tot[k] > 1e-6f) {
+            const float inv = __frcp_rn(tot[k]);
+            out[idx] = make_float4(sr[k] * inv, sg[k] * inv, sb[k] * inv, 1.0f);
+        } else {
+            out[idx] = make_float4(cc[k].x, cc[k].y, cc[k].z, 1.0f);
+        }
     }
 }
 
 template <int kStep>
-__global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(const float4 *__restrict__ in,
+__global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(const float4 *__restrict__ in,
                                                                            float4 *__restrict__ out,
                                                                            const float4 *__restrict__ gbuffer,
                                                                            const float4 *__restrict__ moments,
@@ -221,27 +238,43 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY) denoise_tiled_kernel(cons
     const int lx = (int)threadIdx.x, x = x0 + lx, y0 = y0t + r0;
     const float alpha = alpha_dev ? *alpha_dev : p.alpha;
     const float ema_scale = alpha / fmaxf(2.0f - alpha, 1e-4f);
-    float varc[kDnPix];
-#pragma unroll
-    for (int k = 0; k < kDnPix; ++k) {
-        float acc = 0.0f, cnt = 0.0f;
-#pragma unroll
-        for (int qy = 0; qy < 3; ++qy)
-#pragma unroll
-            for (int qx = 0; qx < 3; ++qx) {
-                const float v = s_var[r0 + k * kStep + qy][lx + qx];
-                if (v >= 0.0f) {
-                    acc += v;
-                    cnt += 1.0f;
-                }
-            }
-        varc[k] = (acc / fmaxf(cnt, 1.0f)) * ema_scale;
-    }
     const bool interior = x0 - H >= 0 && y0t - H >= 0 && x0 + kDnBX + H <= W && y0t + kDnRows + H <= Hh;
-    if (interior)
-        denoise_column<kStep, true>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
-    else
-        denoise_column<kStep, false>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+    float varc[kDnPix];
+    if (interior) {
+        // every 3 x 3 window is inside the image: sums of three per tile row, shared by the
+        // thread's four windows (rows r0 + t, t = 0 .. 3 step + 2)
+        constexpr int kRows = 3 * kStep + 3;
+        float rs[kRows];
+#pragma unroll
+        for (int t = 0; t < kRows; ++t)
+            rs[t] = s_var[r0 + t][lx] + s_var[r0 + t][lx + 1] + s_var[r0 + t][lx + 2];
+        const float scale = ema_scale * (1.0f / 9.0f);
+#pragma unroll
+        for (int k = 0; k < kDnPix; ++k) varc[k] = (rs[k * kStep] + rs[k * kStep + 1] + rs[k * kStep + 2]) * scale;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kDnPix; ++k) {
+            float acc = 0.0f, cnt = 0.0f;
+#pragma unroll
+            for (int qy = 0; qy < 3; ++qy)
+#pragma unroll
+                for (int qx = 0; qx < 3; ++qx) {
+                    const float v = s_var[r0 + k * kStep + qy][lx + qx];
+                    if (v >= 0.0f) {
+                        acc += v;
+                        cnt += 1.0f;
+                    }
+                }
+            varc[k] = (acc / fmaxf(cnt, 1.0f)) * ema_scale;
+        }
+    }
+    if (p.phi_normal == 12.0f) {
+        if (interior) denoise_column<kStep, true, true>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+        else denoise_column<kStep, false, true>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+    } else {
+        if (interior) denoise_column<kStep, true, false>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+        else denoise_column<kStep, false, false>(s_cl, s_nd, varc, lx, r0, x, y0, W, Hh, p, out);
+    }
 }
 
 template <int kStep>
@@ -256,6 +289,7 @@ void prepare_kernels() {
                          (int)denoise_smem_bytes<1>());
     cudaFuncSetAttribute(denoise_tiled_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)denoise_smem_bytes<2>());
+    prepare_wavefront_kernels();
     done = true;
 }
 

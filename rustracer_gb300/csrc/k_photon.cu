@@ -245,7 +245,8 @@ __device__ __forceinline__ uint4 load_keys4(const uint32_t *__restrict__ keys, u
     return k;
 }
 
-// Histogram.  Lanes of a warp holding the same key are merged (match.any) into one atomic.
+// Histogram: one reduction per valid key (no return value, so the adds do not hold the warp; keys of
+// one warp rarely repeat, so merging lanes first costs more than it saves).
 __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                     uint32_t *__restrict__ counts) {
     const uint64_t stride = 4ull * gridDim.x * blockDim.x;
@@ -253,42 +254,32 @@ __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
         const uint4 k4 = load_keys4(keys, start + r * stride, n);
-        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t k = kk[j];
-            uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-            uint32_t leader = __ffs(peers) - 1;
-            if (k != kInvalidKey && (threadIdx.x & 31u) == leader) atomicAdd(counts + k, (uint32_t)__popc(peers));
-        }
+        if (k4.x != kInvalidKey) atomicAdd(counts + k4.x, 1u);
+        if (k4.y != kInvalidKey) atomicAdd(counts + k4.y, 1u);
+        if (k4.z != kInvalidKey) atomicAdd(counts + k4.z, 1u);
+        if (k4.w != kInvalidKey) atomicAdd(counts + k4.w, 1u);
     }
 }
 
-// Slot indices to start[key] + cursor[key]; a warp's lanes with one key take consecutive positions.
+// Slot indices to start[key] + cursor[key] (positions within a cell in atomic order; the order pass
+// restores slot order).
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                       const uint2 *__restrict__ meta, uint32_t *__restrict__ cursor,
                                                       uint32_t *__restrict__ order) {
     const uint64_t stride = 4ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
     const uint64_t rounds = (n + stride - 1) / stride;
-    const uint32_t lane = threadIdx.x & 31u;
     for (uint64_t r = 0; r < rounds; ++r) {
         const uint64_t s0 = start + r * stride;
         const uint4 k4 = load_keys4(keys, s0, n);
         const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+        uint32_t pos[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t k = kk[j];
-            uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-            uint32_t leader = __ffs(peers) - 1;
-            uint32_t base = 0;
-            if (k != kInvalidKey && lane == leader) base = atomicAdd(cursor + k, (uint32_t)__popc(peers));
-            base = __shfl_sync(peers, base, leader);
-            if (k != kInvalidKey) {
-                uint32_t rank = __popc(peers & lanemask_lt());
-                order[__ldg(&meta[k].x) + base + rank] = (uint32_t)(s0 + j);
-            }
-        }
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) pos[j] = atomicAdd(cursor + kk[j], 1u) + __ldg(&meta[kk[j]].x);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)(s0 + j);
     }
 }
 
@@ -365,26 +356,41 @@ __global__ void __launch_bounds__(kScanThreads) scan_partials_kernel(uint32_t *p
 }
 
 // Rescan each tile with its offset; writes (start, count) per cell.  Items are blocked per thread
-// (thread t owns cells t*8 .. t*8+7 of the tile) so the in-thread sums stay in cell order.
+// (thread t owns cells t*8 .. t*8+7 of the tile, two 16-byte loads, four 16-byte stores) so the
+// in-thread sums stay in cell order.
 __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t *__restrict__ counts, uint32_t n,
                                                                   const uint32_t *__restrict__ partials,
-                                                                  uint2 *__restrict__ meta) {
+                                                                  uint2 *__restrict__ meta, bool vec) {
     __shared__ uint32_t warp_sums[kScanThreads / 32];
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
+    if (vec && base + kScanItems <= n) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(counts + base));
+        const uint4 b = __ldg(reinterpret_cast<const uint4 *>(counts + base + 4));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? __ldg(counts + base + i) : 0u;
+    }
     uint32_t local = 0;
 #pragma unroll
-    for (uint32_t i = 0; i < kScanItems; ++i) {
-        uint32_t c = base + i;
-        v[i] = c < n ? __ldg(counts + c) : 0u;
-        local += v[i];
-    }
+    for (uint32_t i = 0; i < kScanItems; ++i) local += v[i];
     uint32_t ex = block_exclusive_scan(local, warp_sums, nullptr) + __ldg(partials + blockIdx.x);
+    uint32_t st[kScanItems];
 #pragma unroll
     for (uint32_t i = 0; i < kScanItems; ++i) {
-        uint32_t c = base + i;
-        if (c < n) meta[c] = make_uint2(ex, v[i]);
+        st[i] = ex;
         ex += v[i];
+    }
+    if (vec && base + kScanItems <= n) {
+        uint4 *m4 = reinterpret_cast<uint4 *>(meta + base);
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; i += 2) m4[i / 2] = make_uint4(st[i], v[i], st[i + 1], v[i + 1]);
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i)
+            if (base + i < n) meta[base + i] = make_uint2(st[i], v[i]);
     }
 }
 
@@ -424,25 +430,93 @@ __device__ __forceinline__ void warp_bitonic(Seg seg, uint32_t count, uint32_t l
 constexpr uint32_t kOrderWarps = 8;
 constexpr uint32_t kOrderSmem = 1024;  // per-warp shared buffer (entries)
 
-// Cells holding two or more photons, appended to `list` (one thread per cell, coalesced meta reads).
-__global__ void __launch_bounds__(256) multi_cells_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
-                                                          uint32_t *__restrict__ list, uint32_t *__restrict__ n_list) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n_cells + stride - 1) / stride;
-    for (uint32_t r = 0; r < rounds; ++r) {
-        const uint32_t c = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool want = c < n_cells && __ldg(&meta[c].y) > 1u;
-        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
-        if (mask == 0u) continue;
-        const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(n_list, (uint32_t)__popc(mask));
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
-        if (want) list[base + __popc(mask & lanemask_lt())] = c;
+// Ascending bitonic sort of 32 * R values held R per lane (value e = lane * R + r).  Exchanges at
+// distance j < R stay in the lane's registers; wider ones pair lanes lane ^ (j / R) by shuffle.
+template <int R>
+__device__ __forceinline__ void warp_sort_regs(uint32_t (&v)[R], uint32_t lane) {
+#pragma unroll
+    for (uint32_t k = 2; k <= 32u * R; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= (uint32_t)R) {
+                const uint32_t lj = j / R;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t e = lane * R + r;
+                    const uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[r], lj);
+                    const bool up = (e & k) == 0u, lower = (e & j) == 0u;
+                    v[r] = (lower == up) ? min(v[r], o) : max(v[r], o);
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int q = r ^ (int)j;
+                    if (q > r) {
+                        const uint32_t e = lane * R + r;
+                        const bool up = (e & k) == 0u;
+                        const uint32_t a = v[r], b = v[q];
+                        v[r] = up ? min(a, b) : max(a, b);
+                        v[q] = up ? max(a, b) : min(a, b);
+                    }
+                }
+            }
+        }
     }
 }
 
-// One warp per listed cell: the cell's slot indices sorted ascending.
+// Sorts the cell's `count` (<= 32 R) slot indices order[start ..] in place.
+template <int R>
+__device__ __forceinline__ void sort_cell_regs(uint32_t *__restrict__ order, uint32_t start, uint32_t count,
+                                               uint32_t lane) {
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = lane * R + r;
+        v[r] = e < count ? order[start + e] : 0xFFFFFFFFu;
+    }
+    warp_sort_regs<R>(v, lane);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = lane * R + r;
+        if (e < count) order[start + e] = v[r];
+    }
+}
+
+// Cells holding two or more photons, appended to `list` (two cells per 16-byte meta load).
+__global__ void __launch_bounds__(256) multi_cells_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
+                                                          uint32_t *__restrict__ list, uint32_t *__restrict__ n_list,
+                                                          bool vec) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n_pairs = (n_cells + 1u) / 2u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n_pairs + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t pr = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const uint32_t c0 = 2u * pr;
+        uint32_t n0 = 0, n1 = 0;
+        if (vec && c0 + 1u < n_cells) {
+            const uint4 m = __ldg(reinterpret_cast<const uint4 *>(meta + c0));
+            n0 = m.y;
+            n1 = m.w;
+        } else {
+            if (c0 < n_cells) n0 = __ldg(&meta[c0].y);
+            if (c0 + 1u < n_cells) n1 = __ldg(&meta[c0 + 1u].y);
+        }
+        const bool w0 = n0 > 1u, w1 = n1 > 1u;
+        const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, w0), m1 = __ballot_sync(0xFFFFFFFFu, w1);
+        const uint32_t tot = __popc(m0) + __popc(m1);
+        if (tot == 0u) continue;
+        uint32_t base = 0;
+        if (lane == 0u) base = atomicAdd(n_list, tot);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        const uint32_t lt = lanemask_lt();
+        if (w0) list[base + __popc(m0 & lt)] = c0;
+        if (w1) list[base + __popc(m0) + __popc(m1 & lt)] = c0 + 1u;
+    }
+}
+
+// One warp per listed cell: the cell's slot indices (in atomic order after the scatter) sorted
+// ascending, so photons of a cell keep slot order, as a sequential scatter would leave them.
 __global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__restrict__ meta,
                                                                   const uint32_t *__restrict__ list,
                                                                   const uint32_t *__restrict__ n_list,
@@ -452,23 +526,17 @@ __global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__
     const uint32_t warps_total = gridDim.x * kOrderWarps;
     const uint32_t n = *n_list;
     for (uint32_t li = blockIdx.x * kOrderWarps + w; li < n; li += warps_total) {
-        const uint32_t c = __ldg(list + li);
-        uint2 m = __ldg(meta + c);
+        const uint2 m = __ldg(meta + __ldg(list + li));
         const uint32_t start = m.x, count = m.y;
         if (count <= 1u) continue;
         if (count <= 32u) {
-            uint32_t v = lane < count ? order[start + lane] : 0xFFFFFFFFu;
-#pragma unroll
-            for (uint32_t k = 2; k <= 32; k <<= 1)
-#pragma unroll
-                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                    uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v, j);
-                    bool up = (lane & k) == 0u;
-                    bool lower = (lane & j) == 0u;
-                    uint32_t mn = min(v, o), mx = max(v, o);
-                    v = (lower == up) ? mn : mx;
-                }
-            if (lane < count) order[start + lane] = v;
+            sort_cell_regs<1>(order, start, count, lane);
+        } else if (count <= 64u) {
+            sort_cell_regs<2>(order, start, count, lane);
+        } else if (count <= 128u) {
+            sort_cell_regs<4>(order, start, count, lane);
+        } else if (count <= 256u) {
+            sort_cell_regs<8>(order, start, count, lane);
         } else if (count <= kOrderSmem) {
             uint32_t *sb = buf[w];
             for (uint32_t i = lane; i < count; i += 32) sb[i] = order[start + i];
@@ -482,20 +550,38 @@ __global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__
     }
 }
 
-// sorted[i] = photons[order[i]] for i < total.
+// sorted[i] = photons[order[i]] for i < total; two photons per thread, all eight 16-byte loads
+// issued before the stores.
 __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__restrict__ photons,
                                                             const uint32_t *__restrict__ order,
                                                             const uint32_t *__restrict__ total, uint64_t cap,
                                                             float4 *__restrict__ sorted) {
     const uint64_t n = min((uint64_t)__ldg(total), cap);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const float4 *src = photons + 4ull * __ldg(order + i);
-        float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
-        float4 *dst = sorted + 4ull * i;
-        dst[0] = a;
-        dst[1] = b;
-        dst[2] = c;
-        dst[3] = d;
+    const uint64_t stride = 2ull * gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t i2 = i + (uint64_t)gridDim.x * blockDim.x;
+        const float4 *s0 = photons + 4ull * __ldg(order + i);
+        const float4 a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + 2), d = __ldg(s0 + 3);
+        float4 e = a, f = b, g = c, h = d;
+        if (i2 < n) {
+            const float4 *s1 = photons + 4ull * __ldg(order + i2);
+            e = __ldg(s1);
+            f = __ldg(s1 + 1);
+            g = __ldg(s1 + 2);
+            h = __ldg(s1 + 3);
+        }
+        float4 *d0 = sorted + 4ull * i;
+        d0[0] = a;
+        d0[1] = b;
+        d0[2] = c;
+        d0[3] = d;
+        if (i2 < n) {
+            float4 *d1 = sorted + 4ull * i2;
+            d1[0] = e;
+            d1[1] = f;
+            d1[2] = g;
+            d1[3] = h;
+        }
     }
 }
 
@@ -512,23 +598,25 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
         return (unsigned)(b < 1 ? 1 : (b < cap ? b : cap));
     };
     if (n) {
-        count_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
+        count_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
+    // 16-byte vector access to counts / meta when the caller's buffers allow it
+    const bool vec = (reinterpret_cast<uintptr_t>(g.counts) % 16u) == 0u && (reinterpret_cast<uintptr_t>(g.meta) % 16u) == 0u;
     const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
     scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
     scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
-    scan_apply_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta);
+    scan_apply_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (n) {
-        scatter_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
+        scatter_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
         // The cells to order are listed in the cursor array (the cursors are spent after the scatter);
         // the list length is total[1].
         if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-        multi_cells_kernel<<<grid_for(C, 256, 8), 256, 0, st>>>(g.meta, C, g.cursor, g.total + 1);
+        multi_cells_kernel<<<grid_for((C + 1) / 2, 256, 8), 256, 0, st>>>(g.meta, C, g.cursor, g.total + 1, vec);
         order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(g.meta, g.cursor,
                                                                                                 g.total + 1, g.order);
-        photon_gather_kernel<<<grid_for(n, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted);
+        photon_gather_kernel<<<grid_for((n + 1) / 2, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

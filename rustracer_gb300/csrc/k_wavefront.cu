@@ -16,6 +16,8 @@
 // reference's order except that a bounce's NEE term lands after that bounce's other terms; floating
 // point addition order is the only difference (an ulp).  The host launches spp * max_bounces
 // iterations; a path extends at most once per iteration, so that bounds every pixel's segments.
+#include <cstring>
+
 #include "rt_kernels.h"
 
 namespace rtd {
@@ -249,12 +251,11 @@ __global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant_
 }
 
 // ------------------------------------------------------------------------------------------------
-// Persistent traversal warps.  A warp takes chunks of kChunk work items with one atomic and hands them
-// to its idle lanes; every lane then advances its traversal by up to kSteps records before the warp
-// refills again, so lanes whose ray finished early pick up new rays instead of idling.
+// Persistent traversal warps.  A warp takes chunks of `chunk` work items with one atomic and hands
+// them to its idle lanes; every lane then advances its traversal by up to `steps` records before the
+// warp refills again, so lanes whose ray finished early pick up new rays instead of idling.  The
+// traversal stack lives in dynamic shared memory, kStack entries per lane, lane-interleaved.
 // ------------------------------------------------------------------------------------------------
-constexpr uint32_t kChunk = 64;
-constexpr int kSteps = 8;
 
 struct WarpFeed {
     uint32_t next = 0, end = 0;
@@ -263,21 +264,21 @@ struct WarpFeed {
 
 // Gives each lane with need == true the next item index (or none when the items ran out).  Every lane
 // of the warp calls it; returns the lane's index or 0xFFFFFFFF.
-__device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n, uint32_t *fetch) {
+__device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n, uint32_t *fetch, uint32_t chunk) {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t mine = 0xFFFFFFFFu;
     uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
     while (mask != 0u && f.more) {
         if (f.next >= f.end) {
             uint32_t base = 0;
-            if (lane == 0u) base = atomicAdd(fetch, kChunk);
+            if (lane == 0u) base = atomicAdd(fetch, chunk);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) {
                 f.more = false;
                 break;
             }
             f.next = base;
-            f.end = min(base + kChunk, n);
+            f.end = min(base + chunk, n);
         }
         const uint32_t avail = f.end - f.next;
         const uint32_t rank = __popc(mask & lanemask_lt());
@@ -292,9 +293,10 @@ __device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n
 }
 
 // extend: closest hit of each queued path (any job: each lane traces its own job's scene).
-template <int kStack>
-__global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
-    __shared__ uint32_t stack_smem[kStack * 128];
+template <int kStack, int kBlock>
+__global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter,
+                                                           uint32_t chunk, uint32_t steps) {
+    extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
@@ -304,7 +306,7 @@ __global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ 
     bool has = false;
     uint32_t slot = 0;
     for (;;) {
-        const uint32_t item = warp_take(feed, !has, n, fetch);
+        const uint32_t item = warp_take(feed, !has, n, fetch, chunk);
         if (item != 0xFFFFFFFFu) {
             slot = q[item];
             const float4 o = p.ro[slot], d = p.rd[slot];
@@ -317,8 +319,8 @@ __global__ void __launch_bounds__(128) wf_extend_kernel(const __grid_constant__ 
             }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
-        for (int k = 0; k < kSteps && has; ++k) {
-            if (trav_step<false>(st, stk, 128u)) {
+        for (uint32_t k = 0; k < steps && has; ++k) {
+            if (trav_step<false>(st, stk, (uint32_t)kBlock)) {
                 p.hit[slot] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
             }
@@ -655,9 +657,10 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
     store_acc(p, slot, A, acc1);
 }
 
-template <int kStack>
-__global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
-    __shared__ uint32_t stack_smem[kStack * 128];
+template <int kStack, int kBlock>
+__global__ void __launch_bounds__(kBlock) wf_shadow_kernel(const __grid_constant__ WaveParams p, uint32_t iter,
+                                                           uint32_t chunk, uint32_t steps) {
+    extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
     const uint32_t m = p.counts[4 * iter + 1];
     uint32_t *fetch = p.counts + 4 * iter + 3;
@@ -667,7 +670,7 @@ __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ 
     uint32_t rec_i = 0;
     float limit = 0.0f;
     for (;;) {
-        const uint32_t item = warp_take(feed, !has, m, fetch);
+        const uint32_t item = warp_take(feed, !has, m, fetch, chunk);
         if (item != 0xFFFFFFFFu) {
             rec_i = item;
             const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1];
@@ -684,8 +687,9 @@ __global__ void __launch_bounds__(128) wf_shadow_kernel(const __grid_constant__ 
             }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
-        for (int k = 0; k < kSteps && has; ++k) {
-            const bool done = any_hit ? trav_step<true>(st, stk, 128u) : trav_step<false>(st, stk, 128u);
+        for (uint32_t k = 0; k < steps && has; ++k) {
+            const bool done = any_hit ? trav_step<true>(st, stk, (uint32_t)kBlock)
+                                      : trav_step<false>(st, stk, (uint32_t)kBlock);
             if (done) {
                 shadow_resolve(p, rec_i, st, limit);
                 has = false;
@@ -757,27 +761,80 @@ __global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t i
 // ------------------------------------------------------------------------------------------------
 // Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
+WaveTuning default_tuning() { return WaveTuning{128u, 8u, 64u, 8u, 32u}; }
+
+bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
+    const WaveTuning in = t;
+    if (t.block_threads != 64u && t.block_threads != 128u && t.block_threads != 256u) t.block_threads = 128u;
+    const uint32_t max_blocks = 2048u / t.block_threads;  // resident threads per SM
+    t.blocks_per_sm = t.blocks_per_sm < 1u ? 1u : (t.blocks_per_sm > max_blocks ? max_blocks : t.blocks_per_sm);
+    t.chunk = t.chunk < 32u ? 32u : (t.chunk > 1024u ? 1024u : (t.chunk + 31u) / 32u * 32u);
+    t.steps = t.steps < 1u ? 1u : (t.steps > 64u ? 64u : t.steps);
+    const uint32_t need = stack_need > t.stack_entries ? stack_need : t.stack_entries;
+    t.stack_entries = need <= 32u ? 32u : (need <= 48u ? 48u : 64u);
+    return std::memcmp(&in, &t, sizeof(t)) == 0;
+}
+
+namespace {
+
+using TravKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t);
+
+template <int kStack, int kBlock>
+void pick(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
+    if ((int)t.stack_entries == kStack && (int)t.block_threads == kBlock) {
+        ext = wf_extend_kernel<kStack, kBlock>;
+        shd = wf_shadow_kernel<kStack, kBlock>;
+    }
+}
+
+void trav_kernels(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
+    ext = shd = nullptr;
+    pick<32, 64>(t, ext, shd);
+    pick<32, 128>(t, ext, shd);
+    pick<32, 256>(t, ext, shd);
+    pick<48, 64>(t, ext, shd);
+    pick<48, 128>(t, ext, shd);
+    pick<48, 256>(t, ext, shd);
+    pick<64, 64>(t, ext, shd);
+    pick<64, 128>(t, ext, shd);
+    pick<64, 256>(t, ext, shd);
+}
+
+}  // namespace
+
+void prepare_wavefront_kernels() {
+    // Stacks above 48 KB per block (64 entries x 256 lanes) need the dynamic shared-memory opt-in.
+    const int bytes = 64 * 256 * (int)sizeof(uint32_t);
+    cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(wf_shadow_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
-                             cudaStream_t st) {
+                             const WaveTuning &tune, cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4 * (size_t)(iters + 1), st)) != cudaSuccess) return e;
     uint64_t slots = 0;
-    bool big_stack = false;
+    uint32_t stack_need = 0;
     for (uint32_t j = 0; j < n_jobs; ++j) {
         const uint32_t tiles = ((jobs[j].width + 7u) / 8u) * ((jobs[j].height + 3u) / 4u);
         wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p, j);
         slots += jobs[j].npix;
-        big_stack = big_stack || jobs[j].stack_cap > 32u;
+        stack_need = jobs[j].stack_cap > stack_need ? jobs[j].stack_cap : stack_need;
     }
-    const uint64_t blocks_needed = (slots + 127u) / 128u;
-    const uint64_t persistent = (uint64_t)num_sms * 8u;
+    WaveTuning t = tune;
+    normalize_tuning(t, stack_need);
+    TravKernel ext, shd;
+    trav_kernels(t, ext, shd);
+    const size_t smem = (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t);
+    const uint64_t blocks_needed = (slots + t.block_threads - 1u) / t.block_threads;
+    const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);
+    const uint64_t shade_needed = (slots + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
+    const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
     for (uint32_t it = 0; it < iters; ++it) {
-        if (big_stack) wf_extend_kernel<64><<<grid, 128, 0, st>>>(p, it);
-        else wf_extend_kernel<32><<<grid, 128, 0, st>>>(p, it);
-        wf_shade_kernel<<<grid, 128, 0, st>>>(p, it);
-        if (big_stack) wf_shadow_kernel<64><<<grid, 128, 0, st>>>(p, it);
-        else wf_shadow_kernel<32><<<grid, 128, 0, st>>>(p, it);
+        ext<<<grid, t.block_threads, smem, st>>>(p, it, t.chunk, t.steps);
+        wf_shade_kernel<<<shade_grid, 128, 0, st>>>(p, it);
+        shd<<<grid, t.block_threads, smem, st>>>(p, it, t.chunk, t.steps);
     }
     for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);
     wf_count_kernel<<<1, 32, 0, st>>>(p, iters);

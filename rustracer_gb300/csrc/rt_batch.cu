@@ -91,6 +91,7 @@ std::vector<unsigned char> BatchEngine::signature(rt_renderer *const *rs, uint32
         put(s, r->marker);
         put(s, base[j]);
     }
+    put(s, tuning);
     return s;
 }
 
@@ -102,7 +103,7 @@ int BatchEngine::enqueue(rt_renderer *const *rs, uint32_t n, uint32_t iters, con
                                   r->scene.stack_cap};
     }
     const rtd::WaveParams wp = path.params(jobs.device(), n, counters.as<unsigned long long>());
-    RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, stream));
+    RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, tuning, stream));
     for (uint32_t j = 0; j < n; ++j)
         if (int st = rt::enqueue_post(rs[j], alpha[j], dev_alpha ? &jobs.device()[j].alpha : nullptr, stream))
             return st;
@@ -207,7 +208,138 @@ int BatchEngine::stats(rt_frame_stats *out) {
     return RT_OK;
 }
 
+int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_frames, float *best_ms) {
+    if (n == 0) {
+        set_error("batch autotune: no jobs");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    trial_frames = std::max(trial_frames, 1u);
+    // Everything a frame changes: each member's image buffers and frame counters, the engine's
+    // counters and frame count.  Saved here, restored after the trials.
+    struct Saved {
+        DevBuf buf[6];
+        uint32_t sample_counter, frames_since_reset;
+        uint64_t frames;
+    };
+    std::vector<Saved> saved(n);
+    for (uint32_t j = 0; j < n; ++j) {
+        rt_renderer *r = rs[j];
+        const DevBuf *src[6] = {&r->d_frame, &r->d_pingpong, &r->d_moments, &r->d_gbuffer, &r->d_accum, &r->d_output};
+        for (int k = 0; k < 6; ++k) {
+            RT_CK(saved[j].buf[k].alloc(src[k]->bytes));
+            RT_CK(cudaMemcpyAsync(saved[j].buf[k].p, src[k]->p, src[k]->bytes, cudaMemcpyDeviceToDevice, r->stream));
+        }
+        saved[j].sample_counter = r->sample_counter;
+        saved[j].frames_since_reset = r->frames_since_reset;
+        saved[j].frames = r->frames;
+    }
+    DevBuf saved_counters;
+    RT_CK(saved_counters.alloc(counters.bytes));
+    RT_CK(cudaMemcpyAsync(saved_counters.p, counters.p, counters.bytes, cudaMemcpyDeviceToDevice, stream));
+    const uint64_t saved_frames = frames;
+    const size_t saved_ring = ring.used;
+    const GraphMode saved_mode = graph_mode;
+    graph_mode = GraphMode::Off;
+
+    uint32_t stack_need = 0;
+    for (uint32_t j = 0; j < n; ++j) stack_need = std::max(stack_need, rs[j]->scene.stack_cap);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RT_CK(cudaEventCreate(&e0));
+    RT_CK(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } evg{e0, e1};
+    std::vector<std::pair<rtd::WaveTuning, float>> tried;
+    auto measure = [&](rtd::WaveTuning t, float *ms) -> int {
+        rtd::normalize_tuning(t, stack_need);
+        for (auto &x : tried)
+            if (std::memcmp(&x.first, &t, sizeof(t)) == 0) {
+                *ms = x.second;
+                return RT_OK;
+            }
+        tuning = t;
+        RT_CK(cudaEventRecord(e0, stream));
+        for (uint32_t f = 0; f < trial_frames; ++f)
+            if (int st = frame(rs, n)) return st;
+        RT_CK(cudaEventRecord(e1, stream));
+        RT_CK(cudaEventSynchronize(e1));
+        RT_CK(cudaEventElapsedTime(ms, e0, e1));
+        tried.push_back({t, *ms});
+        return RT_OK;
+    };
+    rtd::WaveTuning best = tuning;
+    rtd::normalize_tuning(best, stack_need);
+    float best_t = 0.0f;
+    int st = measure(best, &best_t);
+    // Coordinate descent, one pass over the launch-shape dimensions; a change is kept when it is
+    // faster by more than 2% (frame-to-frame noise).
+    const uint32_t blocks[] = {64u, 128u, 256u};
+    const uint32_t per_sm[] = {2u, 4u, 6u, 8u, 12u, 16u, 24u, 32u};
+    const uint32_t stacks[] = {32u, 48u, 64u};
+    const uint32_t chunks[] = {32u, 64u, 128u, 256u};
+    const uint32_t steps[] = {4u, 8u, 16u, 32u};
+    auto sweep = [&](uint32_t rtd::WaveTuning::*field, const uint32_t *vals, size_t nv) {
+        for (size_t i = 0; i < nv && st == RT_OK; ++i) {
+            rtd::WaveTuning t = best;
+            t.*field = vals[i];
+            float ms = 0.0f;
+            st = measure(t, &ms);
+            if (st == RT_OK && ms < best_t * 0.98f) {
+                best = t;
+                rtd::normalize_tuning(best, stack_need);
+                best_t = ms;
+            }
+        }
+    };
+    sweep(&rtd::WaveTuning::block_threads, blocks, 3);
+    sweep(&rtd::WaveTuning::blocks_per_sm, per_sm, 8);
+    sweep(&rtd::WaveTuning::stack_entries, stacks, 3);
+    sweep(&rtd::WaveTuning::chunk, chunks, 4);
+    sweep(&rtd::WaveTuning::steps, steps, 4);
+    tuning = best;
+    graph_mode = saved_mode;
+
+    // Undo the trial frames.
+    for (uint32_t j = 0; j < n; ++j) {
+        rt_renderer *r = rs[j];
+        DevBuf *dst[6] = {&r->d_frame, &r->d_pingpong, &r->d_moments, &r->d_gbuffer, &r->d_accum, &r->d_output};
+        for (int k = 0; k < 6; ++k)
+            RT_CK(cudaMemcpyAsync(dst[k]->p, saved[j].buf[k].p, dst[k]->bytes, cudaMemcpyDeviceToDevice, r->stream));
+        r->sample_counter = saved[j].sample_counter;
+        r->frames_since_reset = saved[j].frames_since_reset;
+        r->frames = saved[j].frames;
+    }
+    RT_CK(cudaMemcpyAsync(counters.p, saved_counters.p, counters.bytes, cudaMemcpyDeviceToDevice, stream));
+    for (uint32_t j = 0; j < n; ++j) RT_CK(cudaStreamSynchronize(rs[j]->stream));
+    RT_CK(cudaStreamSynchronize(stream));
+    frames = saved_frames;
+    ring.used = saved_ring;
+    if (best_ms) *best_ms = best_t / (float)trial_frames;
+    return st;
+}
+
 }  // namespace rt
+
+namespace {
+
+rtd::WaveTuning from_c(const rt_wavefront_tuning &t) {
+    return rtd::WaveTuning{t.block_threads, t.blocks_per_sm, t.chunk, t.steps, t.stack_entries};
+}
+
+void to_c(const rtd::WaveTuning &t, rt_wavefront_tuning *out) {
+    std::memset(out, 0, sizeof(*out));
+    out->block_threads = t.block_threads;
+    out->blocks_per_sm = t.blocks_per_sm;
+    out->chunk = t.chunk;
+    out->steps = t.steps;
+    out->stack_entries = t.stack_entries;
+}
+
+}  // namespace
 
 struct rt_batch {
     std::vector<rt_renderer *> rs;
@@ -287,4 +419,53 @@ extern "C" int rt_batch_get_stats(rt_batch *b, rt_frame_stats *out) {
         return RT_ERR_INVALID_ARGUMENT;
     }
     return b->eng.stats(out);
+}
+
+extern "C" int rt_batch_set_tuning(rt_batch *b, const rt_wavefront_tuning *t) {
+    if (!b || !t) {
+        set_error("rt_batch_set_tuning: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    b->eng.tuning = from_c(*t);
+    rtd::normalize_tuning(b->eng.tuning, 0u);
+    return RT_OK;
+}
+
+extern "C" int rt_batch_get_tuning(rt_batch *b, rt_wavefront_tuning *t) {
+    if (!b || !t) {
+        set_error("rt_batch_get_tuning: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    to_c(b->eng.tuning, t);
+    return RT_OK;
+}
+
+extern "C" int rt_batch_autotune(rt_batch *b, uint32_t trial_frames, rt_wavefront_tuning *best, float *best_ms) {
+    if (!b) {
+        set_error("rt_batch_autotune: null batch");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    rt::clear_error();
+    const int st = b->eng.autotune(b->rs.data(), (uint32_t)b->rs.size(), trial_frames, best_ms);
+    if (best) to_c(b->eng.tuning, best);
+    return st;
+}
+
+extern "C" int rt_set_tuning(rt_renderer *r, const rt_wavefront_tuning *t) {
+    if (!r || !t) {
+        set_error("rt_set_tuning: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    r->tuning = from_c(*t);
+    rtd::normalize_tuning(r->tuning, 0u);
+    return RT_OK;
+}
+
+extern "C" int rt_get_tuning(const rt_renderer *r, rt_wavefront_tuning *t) {
+    if (!r || !t) {
+        set_error("rt_get_tuning: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    to_c(r->tuning, t);
+    return RT_OK;
 }

@@ -23,6 +23,7 @@ struct BatchEngine {
     DevBuf counters;  // [0] segments, [1] shadow rays, summed over all frames
     int num_sms = 1;
     GraphMode graph_mode = GraphMode::Off;
+    rtd::WaveTuning tuning = rtd::default_tuning();
     cudaGraphExec_t exec = nullptr;
     std::vector<unsigned char> sig, last_sig;  // shape of the captured graph; of the previous frame
     std::vector<uint32_t> base;                // first path slot of each member, this frame
@@ -38,6 +39,10 @@ struct BatchEngine {
     // queued on the renderers' own streams; their streams wait for the frame.
     int frame(rt_renderer *const *rs, uint32_t n);
     int stats(rt_frame_stats *out);
+    // Times launch shapes of the traversal kernels on `trial_frames` frames each (coordinate descent
+    // from the current tuning) and keeps the fastest.  The trial frames are undone: each member's
+    // accumulation and frame counters are restored, so the images that follow are unaffected.
+    int autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_frames, float *best_ms);
 
   private:
     std::vector<unsigned char> signature(rt_renderer *const *rs, uint32_t n, uint32_t iters) const;

@@ -45,12 +45,24 @@ struct WaveParams {
 struct JobShape {
     uint32_t width, height, npix, base, stack_cap;
 };
+// Launch shape of the persistent traversal kernels (extend, shadow); no effect on any result.
+struct WaveTuning {
+    uint32_t block_threads;  // 64, 128 or 256
+    uint32_t blocks_per_sm;  // persistent blocks per SM (the grid is capped by the work)
+    uint32_t chunk;          // queue items a warp takes per atomic: its segment of the queue
+    uint32_t steps;          // traversal records between lane refills
+    uint32_t stack_entries;  // shared-memory stack per lane: 32, 48 or 64 (raised to the jobs' need)
+};
+WaveTuning default_tuning();
+// Clamps a tuning to supported values (stack raised to `stack_need`); false if it had to change.
+bool normalize_tuning(WaveTuning &t, uint32_t stack_need);
 // generate (per job), iters x (extend, shade, shadow) over all jobs, finalize (per job), counters.
 cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
-                             cudaStream_t st);
+                             const WaveTuning &tune, cudaStream_t st);
 int device_sm_count();
 // One-time kernel attributes (shared-memory opt-ins); call before capturing launches into a graph.
 void prepare_kernels();
+void prepare_wavefront_kernels();
 
 struct PhotonTraceParams {
     DevScene scene;

@@ -56,7 +56,8 @@ static_assert(sizeof(rt_tonemap_params) == 32 && offsetof(rt_tonemap_params, mar
 // Backend-only structs (no reference counterpart): sizes the ctypes mirror relies on.
 static_assert(sizeof(rt_render_config) == 96, "rt_render_config");
 static_assert(sizeof(rt_camera) == 52, "rt_camera");
-static_assert(sizeof(rt_server_config) == 32, "rt_server_config");
+static_assert(sizeof(rt_wavefront_tuning) == 32, "rt_wavefront_tuning");
+static_assert(sizeof(rt_server_config) == 64, "rt_server_config");
 static_assert(sizeof(rt_request) == 164 && offsetof(rt_request, config) == 16 && offsetof(rt_request, camera) == 112,
               "rt_request");
 static_assert(sizeof(rt_job_status) == 48, "rt_job_status");

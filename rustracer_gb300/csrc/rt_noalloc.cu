@@ -46,6 +46,11 @@ extern "C" int rt_stage_photon_grid_noalloc(const rt_photon *d_photons, const rt
         set_error("rt_stage_photon_grid_noalloc: null argument");
         return RT_ERR_INVALID_ARGUMENT;
     }
+    if ((reinterpret_cast<uintptr_t>(d_photons) | reinterpret_cast<uintptr_t>(d_sorted)) % 16u != 0u ||
+        (reinterpret_cast<uintptr_t>(d_counts) | reinterpret_cast<uintptr_t>(d_meta)) % 4u != 0u) {
+        set_error("rt_stage_photon_grid_noalloc: d_photons / d_sorted must be 16-byte aligned, d_counts / d_meta 4-byte");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
     if (gp->num_cells == 0 || gp->num_cells > RT_NOALLOC_MAX_CELLS || gp->photon_slots > RT_NOALLOC_MAX_SLOTS) {
         set_error("rt_stage_photon_grid_noalloc: %u slots and %u cells requested; this entry point handles at most "
                   "%u slots and %u cells (use rt_stage_photon_grid beyond that)",

@@ -200,6 +200,7 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
         return fail(RT_ERR_OUT_OF_MEMORY);
     }
     r->num_sms = rtd::device_sm_count();
+    rtd::prepare_kernels();
     RT_CK(r->d_output.alloc(npix * 4));
     RT_CK(cudaMemsetAsync(r->d_output.p, 0, npix * 4, s));
     RT_CK(r->d_counters.alloc(64));
@@ -525,7 +526,7 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     RT_CK(r->jobs.upload(&job, 1, s));
     const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
     const rtd::JobShape shape{c.width, c.height, (uint32_t)npix, 0u, r->scene.stack_cap};
-    RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, s));
+    RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
     float4 *result = nullptr;

@@ -201,6 +201,7 @@ struct rt_renderer {
     rt::DevBuf d_frame, d_pingpong, d_moments, d_gbuffer, d_accum, d_output;
     rt::PathState path;  // allocated on the first solo frame (a batch brings its own)
     rt::JobTable jobs;
+    rtd::WaveTuning tuning = rtd::default_tuning();  // solo frames
     int num_sms = 1;
     rt::DevBuf d_photons, d_keys, d_order, d_sorted, d_counts, d_meta, d_cursor, d_partials, d_total, d_counters;
     uint64_t photon_slots = 1;

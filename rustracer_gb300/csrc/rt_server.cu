@@ -412,6 +412,11 @@ extern "C" int rt_server_create(const rt_server_config *cfg, rt_server **out) {
     }
     const rt::GraphMode gm = s->cfg.graphs ? rt::GraphMode::OnRepeat : rt::GraphMode::Off;
     int st = s->eng.init(s->cfg.max_jobs, gm);
+    const rt_wavefront_tuning &tc = s->cfg.tuning;
+    if (tc.block_threads | tc.blocks_per_sm | tc.chunk | tc.steps | tc.stack_entries) {
+        s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk, tc.steps, tc.stack_entries};
+        rtd::normalize_tuning(s->eng.tuning, 0u);
+    }
     if (st == RT_OK) st = s->eng.reserve(s->cfg.max_slots, 64);
     if (st != RT_OK) {
         delete s;

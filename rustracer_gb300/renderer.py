@@ -224,6 +224,16 @@ class Renderer:
     def device_bytes(self) -> int:
         return int(self._lib.rt_renderer_device_bytes(self._h))
 
+    @property
+    def tuning(self) -> dict:
+        t = A.WavefrontTuning()
+        A.check("rt_get_tuning", self._lib.rt_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, values: dict) -> None:
+        A.check("rt_set_tuning", self._lib.rt_set_tuning(self._h, C.byref(tuning_c(values))))
+
     # ---- read-backs ------------------------------------------------------------------------------
     def _img(self, fn: str) -> np.ndarray:
         c = self.config
@@ -271,6 +281,13 @@ class Renderer:
         return counts, meta
 
 
+def tuning_c(values: dict | None) -> A.WavefrontTuning:
+    t = A.WavefrontTuning()
+    for k, v in (values or {}).items():
+        setattr(t, k, int(v))
+    return t
+
+
 class Batch:
     """Renders the next frame of several renderers at once (rt_batch_*); their rays share the same
     wavefront launches.  use_graphs captures each batch frame as a CUDA graph."""
@@ -310,6 +327,23 @@ class Batch:
 
     def stream(self) -> int:
         return int(self._lib.rt_batch_stream(self._h) or 0)
+
+    @property
+    def tuning(self) -> dict:
+        t = A.WavefrontTuning()
+        A.check("rt_batch_get_tuning", self._lib.rt_batch_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, values: dict) -> None:
+        A.check("rt_batch_set_tuning", self._lib.rt_batch_set_tuning(self._h, C.byref(tuning_c(values))))
+
+    def autotune(self, trial_frames: int = 1) -> tuple[dict, float]:
+        """Picks the traversal launch shape by timing trial frames (undone afterwards); returns the
+        chosen shape and its milliseconds per frame."""
+        t, ms = A.WavefrontTuning(), C.c_float()
+        A.check("rt_batch_autotune", self._lib.rt_batch_autotune(self._h, trial_frames, C.byref(t), C.byref(ms)))
+        return t.as_dict(), float(ms.value)
 
 
 def render_config_default() -> RenderConfig:

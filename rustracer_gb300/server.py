@@ -15,13 +15,13 @@ import ctypes as C
 import numpy as np
 
 from . import _abi as A
-from .renderer import RenderConfig
+from .renderer import RenderConfig, tuning_c
 from .scene import Camera, Scene
 
 
 class Server:
     def __init__(self, mode: str = "batched", hbm_cap_bytes: int = 0, max_jobs: int = 0, max_slots: int = 0,
-                 graphs: bool = True, frames_in_flight: int = 0):
+                 graphs: bool = True, frames_in_flight: int = 0, tuning: dict | None = None):
         self._lib = A.load()
         cfg = A.ServerConfig()
         cfg.hbm_cap_bytes = hbm_cap_bytes
@@ -30,6 +30,7 @@ class Server:
         cfg.mode = {"batched": A.SERVER_BATCHED, "plain": A.SERVER_PLAIN}[mode]
         cfg.graphs = int(graphs)
         cfg.frames_in_flight = frames_in_flight
+        cfg.tuning = tuning_c(tuning)
         h = C.c_void_p()
         A.check("rt_server_create", self._lib.rt_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -124,6 +124,7 @@ def test_batch_rejects_bad_arguments(gpu, specs):
 
 def test_resident_scene_shared_by_renderers(gpu, specs):
     scene, cfg, cam, _ = specs[2]  # textured icosphere room with a photon map
+    cam = cam or scene.default_camera()
     res = rt.ResidentScene(scene)
     assert res.refs() == 1 and res.device_bytes() > 0
     create_bytes, path_bytes = res.footprint(cfg)
@@ -145,3 +146,29 @@ def test_resident_scene_shared_by_renderers(gpu, specs):
     a.render_frame()
     a.close()
     b.close()
+
+
+def test_autotune_leaves_images_unchanged(gpu, specs, alone):
+    """Trial frames of the autotuner are undone; any launch shape renders the same images."""
+    rs = [make(sp) for sp in specs]
+    b = rt.Batch(rs, use_graphs=True)
+    b.render_frames(2)
+    best, ms = b.autotune(trial_frames=1)
+    assert ms > 0 and best == b.tuning
+    assert all(r.sample_count() == 2 for r in rs)
+    b.render_frames(3)
+    for j, r in enumerate(rs):
+        assert same(outputs(r), alone[j][0]), f"job {j}"
+    b.close()
+
+
+@pytest.mark.parametrize("shape", [dict(block_threads=64, blocks_per_sm=16, chunk=32, steps=4, stack_entries=48),
+                                   dict(block_threads=256, blocks_per_sm=4, chunk=256, steps=32, stack_entries=64)])
+def test_launch_shape_does_not_change_images(gpu, specs, alone, shape):
+    rs = [make(sp) for sp in specs]
+    for r in rs:
+        r.tuning = shape
+        assert r.tuning["block_threads"] == shape["block_threads"]
+        r.render_frames(5)
+    for j, r in enumerate(rs):
+        assert same(outputs(r), alone[j][0]), f"job {j}"

@@ -89,9 +89,9 @@ def test_icosphere_textured_all_materials(gpu, orc):
     assert {0, 1, 2, 3} <= set(np.unique(kinds).tolist())
 
 
-def test_denoise_stage(gpu, orc):
+@pytest.mark.parametrize("h,w", [(61, 97), (136, 200)])  # the larger size has tiles away from every border
+def test_denoise_stage(gpu, orc, h, w):
     rng = np.random.default_rng(3)
-    h, w = 61, 97
     frame = rng.random((h, w, 4), np.float32) * 2
     frame[..., 3] = 1
     n = rng.normal(size=(h, w, 3)).astype(np.float32)

@@ -77,7 +77,8 @@ def test_backend_struct_sizes_match_the_header():
     """The ctypes mirrors of the backend-only structs (static_assert'ed in rt_layout_check.h)."""
     assert C.sizeof(A.RenderConfigC) == 96
     assert C.sizeof(A.Camera) == 52
-    assert C.sizeof(A.ServerConfig) == 32
+    assert C.sizeof(A.WavefrontTuning) == 32
+    assert C.sizeof(A.ServerConfig) == 64
     assert C.sizeof(A.Request) == 164
     assert A.Request.config.offset == 16 and A.Request.camera.offset == 112
     assert C.sizeof(A.JobStatus) == 48
