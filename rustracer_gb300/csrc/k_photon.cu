@@ -1,17 +1,22 @@
-// Photon pass of rebuild_photons (rustracer-renderer/src/lib.rs:913-1037):
+// Photon pass and photon grid (config 3 of the photon map).
 //
-//   photon_trace_kernel   photon_trace.wgsl:101-260.  Also emits the u32 cell key of every slot it
-//                         stores (photon_count.wgsl:18-32), so the grid build never re-reads positions.
+//   photon wavefront      photon_trace.wgsl:91-260 as generate (emission) + per bounce the shared
+//                         closest-hit kernel and ph_shade (one bounce body per queued photon).  The
+//                         bounce body also emits the u32 cell key of every slot it stores
+//                         (photon_count.wgsl:18-23), so the grid build never re-reads positions.
 //   photon_keys_kernel    keys of a photon buffer loaded from the host (same key function).
 //   grid build            exact u32 counting sort of the slots by cell key:
-//     count_kernel        histogram (photon_count.wgsl:25-34), warp-aggregated atomics
+//     count_kernel        histogram (photon_count.wgsl:25-34)
 //     scan_*              device exclusive scan of the counts into (start, count) pairs; replaces the
 //                         blocking read-back and host scan of lib.rs:956-1007
-//     scatter_kernel      slot index to start + cursor (photon_scatter.wgsl:61-71), warp-aggregated
-//     order_kernel        sorts each cell's slot indices ascending: the result is the scatter in slot
-//                         order, independent of atomic arrival order (the reference's order within a
-//                         cell is unspecified)
+//     scatter_kernel      slot index to start + cursor (photon_scatter.wgsl:61-71)
+//     multi_cells_kernel  the cells holding two or more photons
+//     order_kernel        sorts each such cell's slot indices ascending: the result is the scatter in
+//                         slot order, independent of atomic arrival order (the reference's order
+//                         within a cell is unspecified)
 //     gather_kernel       sorted[i] = photons[order[i]] (64-byte records)
+#include <cstring>
+
 #include "rt_kernels.h"
 
 namespace rtd {
@@ -51,27 +56,27 @@ __device__ __forceinline__ uint32_t slot_key(const rt_grid_params &gp, f3 pos, f
 
 constexpr int kTraceBlock = 128;
 
-__global__ void __launch_bounds__(kTraceBlock) photon_trace_kernel(const __grid_constant__ PhotonTraceParams p) {
-    __shared__ uint32_t stack_smem[64 * kTraceBlock];
-    uint32_t *stk = stack_smem + threadIdx.x;
-    const uint32_t stride = kTraceBlock;
-    const uint32_t photon_index = p.photon_begin + blockIdx.x * kTraceBlock + threadIdx.x;
-    if (photon_index >= p.photon_end) return;
+// The photon's origin, direction and power as emitted from a light picked uniformly
+// (photon_trace.wgsl:91-190); false when no photon leaves (no lights, unknown kind).
+__device__ bool photon_emit(const PhotonTraceParams &p, uint32_t photon_index, Rng &rng, f3 &origin, f3 &dir,
+                            f3 &power) {
     const DevScene &s = p.scene;
     const uint32_t num_lights = s.light_count;
-    if (num_lights == 0u) return;
-    Rng rng = rng_init(photon_index * 1103515245u + 12345u);
+    if (num_lights == 0u) return false;
+    rng = rng_init(photon_index * 1103515245u + 12345u);
     uint32_t li = f2u_sat(rng_f32(rng) * (float)num_lights);
     li = li < num_lights ? li : num_lights - 1u;
     const Light light = load_light(s, li);
-    f3 origin = light.data, dir = mk3(0.0f, 0.0f, 1.0f), power = mk3(0.0f, 0.0f, 0.0f);
+    origin = light.data;
+    dir = mk3(0.0f, 0.0f, 1.0f);
+    power = mk3(0.0f, 0.0f, 0.0f);
     if (light.kind == 0u) {
         float u1 = 0.0f, u2 = 0.0f;
         for (uint32_t guard = 0;; ++guard) {
             u1 = rng_f32(rng) * 2.0f - 1.0f;
             u2 = rng_f32(rng) * 2.0f - 1.0f;
             if (u1 * u1 + u2 * u2 < 1.0f) break;
-            if (guard >= (1u << 20)) return;  // bounded; (1 - pi/4)^(2^20) is zero in practice
+            if (guard >= (1u << 20)) return false;  // bounded; (1 - pi/4)^(2^20) is zero in practice
         }
         float z = 1.0f - 2.0f * (u1 * u1 + u2 * u2);
         float r = sqrtf(1.0f - z * z);
@@ -112,89 +117,192 @@ __global__ void __launch_bounds__(kTraceBlock) photon_trace_kernel(const __grid_
         float t = clampf(d.y * 0.5f + 0.5f, 0.0f, 1.0f);
         power = mix3(light.color, light.data, powf(t, 0.5f)) * light.intensity;
     } else {
-        return;
+        return false;
     }
+    return true;
 
-    for (uint32_t bounce = 0; bounce < RT_MAX_BOUNCES; ++bounce) {
-        Hit hit = trace<false>(s, origin, dir, kInf, stk, stride);
-        if (hit.t >= kInf) return;
-        TriFull tri = load_tri(s, hit.prim);
-        Mat mat = load_mat(s, tri.material_id);
-        f3 hit_pos = origin + dir * hit.t;
-        Bary bb = barycentric(tri, origin, dir, hit.t);
-        f3 normal = triangle_normal(tri.v0, tri.v1, tri.v2);
-        bool front = dot(dir, normal) < 0.0f;
-        f3 sn_geom = smooth_normal(tri, bb, normal);
-        f3 face_normal = front ? sn_geom : -sn_geom;
-        f3 shn = face_normal;
-        if (mat.tex_normal != RT_TEX_NONE) {
-            float4 t = tex_sample(s.tex[RT_TEX_NORMAL], bb.uvx, bb.uvy, (int32_t)mat.tex_normal);
-            f3 nm = mk3(t.x, t.y, t.z) * 2.0f - mk3(1.0f, 1.0f, 1.0f);
-            f3 ft, fb;
-            tangent_frame(tri, face_normal, ft, fb);
-            shn = normalize(ft * nm.x + fb * nm.y + face_normal * nm.z);
+}
+
+// One iteration of photon_trace.wgsl's bounce loop (:192-258) after the closest hit (t, prim) of
+// (origin, dir): stores the photon at slot 6 i + bounce unless the surface passes it on, and updates
+// the ray; false when the photon ends (emitter hit, Russian roulette).
+__device__ bool photon_bounce(const PhotonTraceParams &p, uint32_t photon_index, uint32_t bounce, float hit_t,
+                              uint32_t hit_prim, Rng &rng, f3 &origin, f3 &dir, f3 &power) {
+    const DevScene &s = p.scene;
+    struct {
+        float t;
+        uint32_t prim;
+    } hit{hit_t, hit_prim};
+    TriFull tri = load_tri(s, hit.prim);
+    Mat mat = load_mat(s, tri.material_id);
+    f3 hit_pos = origin + dir * hit.t;
+    Bary bb = barycentric(tri, origin, dir, hit.t);
+    f3 normal = triangle_normal(tri.v0, tri.v1, tri.v2);
+    bool front = dot(dir, normal) < 0.0f;
+    f3 sn_geom = smooth_normal(tri, bb, normal);
+    f3 face_normal = front ? sn_geom : -sn_geom;
+    f3 shn = face_normal;
+    if (mat.tex_normal != RT_TEX_NONE) {
+        float4 t = tex_sample(s.tex[RT_TEX_NORMAL], bb.uvx, bb.uvy, (int32_t)mat.tex_normal);
+        f3 nm = mk3(t.x, t.y, t.z) * 2.0f - mk3(1.0f, 1.0f, 1.0f);
+        f3 ft, fb;
+        tangent_frame(tri, face_normal, ft, fb);
+        shn = normalize(ft * nm.x + fb * nm.y + face_normal * nm.z);
+    }
+    if ((mat.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && mat.tex_albedo != RT_TEX_NONE) {
+        float alpha = tex_sample(s.tex[RT_TEX_ALBEDO], bb.uvx, bb.uvy, (int32_t)mat.tex_albedo).w;
+        if (alpha < 0.5f) {
+            origin = hit_pos + dir * 0.002f;
+            return true;
         }
-        if ((mat.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && mat.tex_albedo != RT_TEX_NONE) {
-            float alpha = tex_sample(s.tex[RT_TEX_ALBEDO], bb.uvx, bb.uvy, (int32_t)mat.tex_albedo).w;
-            if (alpha < 0.5f) {
-                origin = hit_pos + dir * 0.002f;
-                continue;
-            }
-        }
-        if (mat.tex_emissive != RT_TEX_NONE || len3(mat.emissive) > 1e-4f || mat.kind == 3u) return;
-        if (mat.kind == 2u) {
-            float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
-            float f0s = powf(q, 2.0f);
-            float ct = fabsf(dot(dir, face_normal));
-            float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
-            if (rng_f32(rng) < fr) {
-                dir = reflect(dir, face_normal);
-                origin = hit_pos + face_normal * 0.001f;
-            } else {
-                float eta = front ? 1.0f / mat.ior : mat.ior;
-                dir = refract(dir, face_normal, eta);
-                origin = hit_pos - face_normal * 0.001f;
-            }
-            continue;
-        }
-        const uint64_t slot = (uint64_t)photon_index * 6u + bounce;
-        if (slot < p.slot_count) {
-            float4 *ph = p.photons + 4ull * slot;
-            f3 inc = -dir;
-            ph[0] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.0f);
-            ph[1] = make_float4(power.x, power.y, power.z, 0.0f);
-            ph[2] = make_float4(inc.x, inc.y, inc.z, 0.0f);
-            ph[3] = make_float4(shn.x, shn.y, shn.z, 0.0f);
-            p.keys[slot] = slot_key(p.gp, hit_pos, power.x);
-        }
-        f3 albedo = surface_albedo(s, mat, bb.uvx, bb.uvy);
-        const float mt = mat.metallic;
-        f3 f0 = mk3(0.04f * (1.0f - mt) + albedo.x * mt, 0.04f * (1.0f - mt) + albedo.y * mt,
-                    0.04f * (1.0f - mt) + albedo.z * mt);
-        float ct = fabsf(dot(dir, shn));
-        f3 fr = fresnel_schlick(ct, f0);
-        f3 diffuse_weight = (1.0f - mt) * albedo;
-        float spec_prob = clampf(max3(fr), 0.0f, 0.98f);
-        bool do_spec = rng_f32(rng) < spec_prob;
-        if (do_spec) {
-            dir = bounce_dir(dir, shn, mat.roughness, rng);
-            power = power * f0;
+    }
+    if (mat.tex_emissive != RT_TEX_NONE || len3(mat.emissive) > 1e-4f || mat.kind == 3u) return false;
+    if (mat.kind == 2u) {
+        float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
+        float f0s = powf(q, 2.0f);
+        float ct = fabsf(dot(dir, face_normal));
+        float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
+        if (rng_f32(rng) < fr) {
+            dir = reflect(dir, face_normal);
+            origin = hit_pos + face_normal * 0.001f;
         } else {
-            f3 local = sample_cosine_hemisphere(rng);
-            dir = to_world(local, shn);
-            power = power * diffuse_weight;
+            float eta = front ? 1.0f / mat.ior : mat.ior;
+            dir = refract(dir, face_normal, eta);
+            origin = hit_pos - face_normal * 0.001f;
         }
-        origin = hit_pos + shn * 0.001f;
-        float pr = max3(power);
-        if (pr <= 0.0f || rng_f32(rng) > pr) return;
-        power = power / pr;
+        return true;
+    }
+    const uint64_t slot = (uint64_t)photon_index * 6u + bounce;
+    if (slot < p.slot_count) {
+        float4 *ph = p.photons + 4ull * slot;
+        f3 inc = -dir;
+        ph[0] = make_float4(hit_pos.x, hit_pos.y, hit_pos.z, 0.0f);
+        ph[1] = make_float4(power.x, power.y, power.z, 0.0f);
+        ph[2] = make_float4(inc.x, inc.y, inc.z, 0.0f);
+        ph[3] = make_float4(shn.x, shn.y, shn.z, 0.0f);
+        p.keys[slot] = slot_key(p.gp, hit_pos, power.x);
+    }
+    f3 albedo = surface_albedo(s, mat, bb.uvx, bb.uvy);
+    const float mt = mat.metallic;
+    f3 f0 = mk3(0.04f * (1.0f - mt) + albedo.x * mt, 0.04f * (1.0f - mt) + albedo.y * mt,
+                0.04f * (1.0f - mt) + albedo.z * mt);
+    float ct = fabsf(dot(dir, shn));
+    f3 fr = fresnel_schlick(ct, f0);
+    f3 diffuse_weight = (1.0f - mt) * albedo;
+    float spec_prob = clampf(max3(fr), 0.0f, 0.98f);
+    bool do_spec = rng_f32(rng) < spec_prob;
+    if (do_spec) {
+        dir = bounce_dir(dir, shn, mat.roughness, rng);
+        power = power * f0;
+    } else {
+        f3 local = sample_cosine_hemisphere(rng);
+        dir = to_world(local, shn);
+        power = power * diffuse_weight;
+    }
+    origin = hit_pos + shn * 0.001f;
+    float pr = max3(power);
+    if (pr <= 0.0f || rng_f32(rng) > pr) return false;
+    power = power / pr;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Photon wavefront: generate (emission), then per bounce the shared closest-hit kernel (wf_extend,
+// persistent traversal warps) and ph_shade (one bounce body per queued photon, survivors re-queued).
+// Lanes stay busy when photons end at different bounces, and each kernel is small; the per-photon
+// operations and their order are those of the loop, so every photon's path is unchanged.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) ph_generate_kernel(const __grid_constant__ PhotonTraceParams p,
+                                                          const PhotonWave w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t photon_index = p.photon_begin + i;
+    bool live = false;
+    if (photon_index < p.photon_end) {
+        Rng rng;
+        f3 origin, dir, power;
+        live = photon_emit(p, photon_index, rng, origin, dir, power);
+        if (live) {
+            w.ro[i] = make_float4(origin.x, origin.y, origin.z, __uint_as_float(rng.state));
+            w.rd[i] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(photon_index));
+            w.pw[i] = make_float4(power.x, power.y, power.z, __uint_as_float(0u));
+        }
+    }
+    warp_append(live, i, w.queue[0], w.counts + 0);
+}
+
+__global__ void __launch_bounds__(128) ph_shade_kernel(const __grid_constant__ PhotonTraceParams p, const PhotonWave w,
+                                                       uint32_t iter) {
+    const uint32_t n = w.counts[4 * iter];
+    const uint32_t *q = w.queue[iter & 1u];
+    const bool last = iter + 1u >= RT_MAX_BOUNCES;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1u) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t item = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool live = false;
+        uint32_t slot = 0;
+        if (item < n) {
+            slot = q[item];
+            const float2 h = w.hit[slot];
+            if (h.x < kInf) {
+                const float4 o = w.ro[slot], d = w.rd[slot], pw = w.pw[slot];
+                Rng rng;
+                rng.state = __float_as_uint(o.w);
+                f3 origin = xyz(o), dir = xyz(d), power = xyz(pw);
+                live = photon_bounce(p, __float_as_uint(d.w), iter, h.x, __float_as_uint(h.y), rng, origin, dir,
+                                     power) && !last;
+                if (live) {
+                    w.ro[slot] = make_float4(origin.x, origin.y, origin.z, __uint_as_float(rng.state));
+                    w.rd[slot] = make_float4(dir.x, dir.y, dir.z, d.w);
+                    w.pw[slot] = make_float4(power.x, power.y, power.z, pw.w);
+                }
+            }
+        }
+        if (!last) warp_append(live, slot, w.queue[(iter + 1u) & 1u], w.counts + 4 * (iter + 1u));
     }
 }
 
-cudaError_t launch_photon_trace(const PhotonTraceParams &p, cudaStream_t st) {
+size_t photon_wave_bytes(uint32_t n) {
+    return (size_t)n * (16 + 16 + 16 + 8 + 4 + 4) + sizeof(uint32_t) * 4 * (RT_MAX_BOUNCES + 1) + 64;
+}
+
+PhotonWave photon_wave_at(void *base, uint32_t n) {
+    unsigned char *b = static_cast<unsigned char *>(base);
+    PhotonWave w;
+    w.ro = reinterpret_cast<float4 *>(b);
+    w.rd = reinterpret_cast<float4 *>(b + 16ull * n);
+    w.pw = reinterpret_cast<float4 *>(b + 32ull * n);
+    w.hit = reinterpret_cast<float2 *>(b + 48ull * n);
+    w.queue[0] = reinterpret_cast<uint32_t *>(b + 56ull * n);
+    w.queue[1] = reinterpret_cast<uint32_t *>(b + 60ull * n);
+    w.counts = reinterpret_cast<uint32_t *>(b + ((64ull * n + 15ull) & ~15ull));
+    return w;
+}
+
+cudaError_t launch_photon_wave(const PhotonTraceParams &p, const PhotonWave &w, const DevJob *jobs_dev, int num_sms,
+                               const WaveTuning &tune, cudaStream_t st) {
     if (p.photon_end <= p.photon_begin) return cudaSuccess;
-    uint32_t n = p.photon_end - p.photon_begin;
-    photon_trace_kernel<<<(n + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0, st>>>(p);
+    const uint32_t n = p.photon_end - p.photon_begin;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(w.counts, 0, sizeof(uint32_t) * 4 * (RT_MAX_BOUNCES + 1), st)) != cudaSuccess) return e;
+    ph_generate_kernel<<<(n + 255u) / 256u, 256, 0, st>>>(p, w);
+    WaveParams wp;
+    std::memset(&wp, 0, sizeof(wp));
+    wp.jobs = jobs_dev;
+    wp.n_jobs = 1;
+    wp.ro = w.ro;
+    wp.rd = w.rd;
+    wp.thr = w.pw;
+    wp.hit = w.hit;
+    wp.queue[0] = w.queue[0];
+    wp.queue[1] = w.queue[1];
+    wp.counts = w.counts;
+    const uint64_t shade_needed = (n + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
+    const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
+    for (uint32_t it = 0; it < RT_MAX_BOUNCES; ++it) {
+        if ((e = launch_extend(wp, it, n, p.scene.stack_cap, num_sms, tune, st)) != cudaSuccess) return e;
+        ph_shade_kernel<<<shade_grid, 128, 0, st>>>(p, w, it);
+    }
     return cudaGetLastError();
 }
 
@@ -229,12 +337,6 @@ cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const
 // ------------------------------------------------------------------------------------------------
 // Grid build
 // ------------------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
 // Four consecutive keys per thread (one 16-byte load when aligned and complete).
 __device__ __forceinline__ uint4 load_keys4(const uint32_t *__restrict__ keys, uint64_t s, uint64_t n) {
     if (s + 3 < n) return __ldg(reinterpret_cast<const uint4 *>(keys + s));

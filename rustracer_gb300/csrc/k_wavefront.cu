@@ -194,25 +194,6 @@ __device__ __forceinline__ void camera_ray(const DevJob &job, uint32_t px, uint3
                    mk3(cam.right[0], cam.right[1], cam.right[2]) * ux + mk3(cam.up[0], cam.up[1], cam.up[2]) * uy);
 }
 
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-// Appends `item` to queue (count at *counter) for the lanes with want == true; one atomic per warp.
-// Every lane of the warp must call it.
-__device__ __forceinline__ void warp_append(bool want, uint32_t item, uint32_t *queue, uint32_t *counter) {
-    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
-    if (mask == 0u) return;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t leader = __ffs(mask) - 1u;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (want) queue[base + __popc(mask & lanemask_lt())] = item;
-}
-
 __device__ __forceinline__ uint32_t pack_sb(uint32_t s, uint32_t b) { return (s & 0xFFFFu) | (b << 16); }
 
 }  // namespace
@@ -807,6 +788,20 @@ void prepare_wavefront_kernels() {
     const int bytes = 64 * 256 * (int)sizeof(uint32_t);
     cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(wf_shadow_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
+                          const WaveTuning &tune, cudaStream_t st) {
+    WaveTuning t = tune;
+    normalize_tuning(t, stack_need);
+    TravKernel ext, shd;
+    trav_kernels(t, ext, shd);
+    const size_t smem = (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t);
+    const uint64_t blocks_needed = (max_items + t.block_threads - 1u) / t.block_threads;
+    const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
+    const uint32_t grid = (uint32_t)(blocks_needed < persistent ? (blocks_needed ? blocks_needed : 1u) : persistent);
+    ext<<<grid, t.block_threads, smem, st>>>(p, iter, t.chunk, t.steps);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,

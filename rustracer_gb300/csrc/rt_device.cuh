@@ -422,4 +422,24 @@ __device__ __forceinline__ void tangent_frame(const TriFull &tri, f3 n, f3 &t_ou
 }
 __device__ __forceinline__ f3 triangle_normal(f3 v0, f3 v1, f3 v2) { return normalize(cross(v1 - v0, v2 - v0)); }
 
+// Warp helpers of the queue kernels.
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Appends `item` to queue (count at *counter) for the lanes with want == true; one atomic per warp.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warp_append(bool want, uint32_t item, uint32_t *queue, uint32_t *counter) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (mask == 0u) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (want) queue[base + __popc(mask & lanemask_lt())] = item;
+}
+
 }  // namespace rtd

@@ -72,10 +72,27 @@ struct PhotonTraceParams {
     float4 *photons;                    // 4 x float4 per slot
     uint32_t *keys;                     // cell key per slot (kInvalidKey when not binned)
 };
-__global__ void photon_trace_kernel(const __grid_constant__ PhotonTraceParams p);
+// State of the photon wavefront, one entry per traced photon (index - photon_begin).
+struct PhotonWave {
+    float4 *ro;        // origin, .w = RNG state
+    float4 *rd;        // direction, .w = photon index
+    float4 *pw;        // power, .w = job index 0 (read by the shared closest-hit kernel)
+    float2 *hit;       // closest t, primitive
+    uint32_t *queue[2];
+    uint32_t *counts;  // 4 per bounce (+1): [0] photons queued, [2] fetch cursor of the hit kernel
+};
+// Bytes of PhotonWave state for n photons (carved from one buffer, 16-byte aligned parts).
+size_t photon_wave_bytes(uint32_t n);
+PhotonWave photon_wave_at(void *base, uint32_t n);
 
 // Launchers (stream-ordered, no synchronisation).  Each returns the launch error, if any.
-cudaError_t launch_photon_trace(const PhotonTraceParams &p, cudaStream_t st);
+// The photon pass (photon_trace.wgsl:91-260) as a wavefront: jobs_dev[0].scene must be p.scene.
+cudaError_t launch_photon_wave(const PhotonTraceParams &p, const PhotonWave &w, const DevJob *jobs_dev, int num_sms,
+                               const WaveTuning &tune, cudaStream_t st);
+// One closest-hit pass of the persistent traversal kernel over queue[iter & 1] (count at
+// counts[4 iter]); `max_items` bounds the grid.
+cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
+                          const WaveTuning &tune, cudaStream_t st);
 
 // Photon grid (exact u32 counting sort).  Scratch sizes come from grid_scratch_bytes.
 struct GridBuffers {

@@ -630,8 +630,17 @@ int rt::enqueue_photon_rebuild(rt_renderer *r) {
     tp.slot_count = r->photon_slots;
     tp.photons = r->d_photons.as<float4>();
     tp.keys = r->d_keys.as<uint32_t>();
+    // The wavefront's state lives in the sorted-photon buffer (6 x 64 B per photon, at least the
+    // 64 B per photon the state needs), which the grid build rewrites afterwards.
+    if (rtd::photon_wave_bytes((uint32_t)traced) > r->d_sorted.bytes) {
+        set_error("rt_rebuild_photons: photon state exceeds the sorted-photon buffer");
+        return RT_ERR_STATE;
+    }
+    const rtd::PhotonWave w = rtd::photon_wave_at(r->d_sorted.p, (uint32_t)traced);
+    const rtd::DevJob job = rt::make_job(r, 0u);
+    RT_CK(r->jobs.upload(&job, 1, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_TRACE0], s));
-    RT_CK(rtd::launch_photon_trace(tp, s));
+    RT_CK(rtd::launch_photon_wave(tp, w, r->jobs.device(), r->num_sms, r->tuning, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_TRACE1], s));
     if (int st = build_grid(r)) return st;
     RT_CK(cudaEventRecord(r->events.ev[EV_GRID1], s));
