@@ -120,6 +120,20 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def job_totals(dist, elapsed: float, *counts: float, device: str = "cpu") -> tuple:
+    """Whole-job figures of a weak-scaling run: the slowest rank's elapsed time and the per-rank counts
+    summed over ranks (all-reduce MAX and SUM; no reduction without a process group)."""
+    import torch
+
+    t = torch.tensor([elapsed, *counts], dtype=torch.float64, device=device)
+    if dist is None:
+        return tuple(float(x) for x in t)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return (float(tmax[0]),) + tuple(float(x) for x in t[1:])
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -210,7 +224,7 @@ def run_reference(args, w):
     cfg = make_config(w)
     cam = scene.default_camera()
     # warm-up samples, then K timed samples (one row band each)
-    per_step = max(1.0, min(20.0, 120.0 / max(args.steps + args.warmup, 1)))
+    per_step = max(0.05, min(20.0, args.ref_seconds / max(args.steps + args.warmup, 1)))
     for _ in range(args.warmup):
         cpu_sample(scene, cfg, cam, per_step / 4, threads)
     vals, descs = [], []
@@ -587,15 +601,7 @@ def run_ours(args, w):
     segments = s1.segments - s0.segments
     shadow = s1.shadow_rays - s0.shadow_rays
 
-    t = torch.tensor([ms, float(segments), float(shadow)], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_max = float(tmax[0])
-    else:
-        ms_max = float(t[0])
-    seg_all, shd_all = float(t[1]), float(t[2])
+    ms_max, seg_all, shd_all = job_totals(dist, ms, float(segments), float(shadow), device="cuda")
     value = seg_all / (ms_max / 1000.0)
 
     # ---- end-to-end through the public API with host buffers --------------------------------
@@ -611,15 +617,8 @@ def run_ours(args, w):
     t1 = time.perf_counter()
     s_e1 = r.stats()
     e2e_seg = float(s_e1.segments - s_e0.segments)
-    e2e_t = torch.tensor([t1 - t0, e2e_seg], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        e_max = e2e_t.clone()
-        dist.all_reduce(e_max, op=dist.ReduceOp.MAX)
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.SUM)
-        e2e_wall = float(e_max[0])
-    else:
-        e2e_wall = float(e2e_t[0])
-    e2e_value = float(e2e_t[1]) / e2e_wall
+    e2e_wall, e2e_seg_all = job_totals(dist, t1 - t0, e2e_seg, device="cuda")
+    e2e_value = e2e_seg_all / e2e_wall
 
     if rank == 0:
         gather_ms = s1.ms_gather_sum / max(s1.timed_frames, 1)
@@ -682,6 +681,8 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="icosphere1080p")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="size of the CPU-baseline sample")
+    ap.add_argument("--ref-seconds", type=float, default=120.0,
+                    help="CPU time of the whole --impl reference run (warm-up and timed samples)")
     ap.add_argument("--no-stages", dest="stages", action="store_false",
                     help="skip the photon-map / denoise stage measurements")
     ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the 64-job batch leg")

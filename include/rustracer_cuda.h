@@ -325,6 +325,15 @@ int rt_set_light_marker(rt_renderer *r, const float marker[4], float glow);
 
 /* sample_count (lib.rs:1039-1041). */
 uint32_t rt_sample_count(const rt_renderer *r);
+/* Accumulation checkpoint and resume (no counterpart in the reference; its raw dump is
+ * render_headless.rs:141-147, the accumulation as W*H*4 f32).  A checkpoint is that dump plus the two
+ * frame counters of rt_get_frame_state (sample_counter = rt_sample_count, frames accumulated since
+ * the last reset).  rt_restore_accumulation writes them back into a renderer of the same
+ * configuration, scene and camera (and, with a photon map, after the same rebuild): the frames it
+ * renders next are the frames the checkpointed renderer would have rendered. */
+int rt_get_frame_state(const rt_renderer *r, uint32_t *sample_counter, uint32_t *frames_since_reset);
+int rt_restore_accumulation(rt_renderer *r, const float *rgba, uint64_t n_floats, uint32_t sample_counter,
+                            uint32_t frames_since_reset);
 int rt_synchronize(rt_renderer *r);
 /* Waits for the renderer's stream.  Per-kernel sums cover the frames since the previous call. */
 int rt_get_stats(rt_renderer *r, rt_frame_stats *out);

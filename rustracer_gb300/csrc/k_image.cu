@@ -102,12 +102,12 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
                                                int lx, int ly0, int x, int y0, int W, int Hh, const rt_denoise_params &p,
                                                float4 *__restrict__ out) {
     constexpr int H = 2 * kStep;
-    float4 cc[kDnPix], cn[kDnPix];
-    float a_l[kDnPix], a_d[kDnPix];
+    float4 cn[kDnPix];
+    float c_lum[kDnPix], a_l[kDnPix], a_d[kDnPix];
     float sr[kDnPix], sg[kDnPix], sb[kDnPix], tot[kDnPix];
 #pragma unroll
     for (int k = 0; k < kDnPix; ++k) {
-        cc[k] = s_cl[ly0 + H + k * kStep][lx + H];
+        c_lum[k] = s_cl[ly0 + H + k * kStep][lx + H].w;
         cn[k] = s_nd[ly0 + H + k * kStep][lx + H];
         a_l[k] = -kLog2e * __frcp_rn(s_varc[k] * p.lambda + 1e-6f);
         a_d[k] = -kLog2e * __frcp_rn(p.phi_depth * fmaxf(cn[k].w, 1e-4f));
@@ -139,7 +139,7 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
                 } else {
                     nw = powf(d, p.phi_normal);
                 }
-                const float dl = nb.w - cc[k].w;
+                const float dl = nb.w - c_lum[k];
                 const float lsw = log_b3(dx < 0 ? -dx : dx) + log_b3(dy < 0 ? -dy : dy);
                 float t = fmaf(fabsf(cn[k].w - nd.w), a_d[k], lsw);
                 t = fmaf(dl * a_l[k], dl, t);
@@ -160,7 +160,8 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
             const float inv = __frcp_rn(tot[k]);
             out[idx] = make_float4(sr[k] * inv, sg[k] * inv, sb[k] * inv, 1.0f);
         } else {
-            out[idx] = make_float4(cc[k].x, cc[k].y, cc[k].z, 1.0f);
+            const float4 c = s_cl[ly0 + H + k * kStep][lx + H];
+            out[idx] = make_float4(c.x, c.y, c.z, 1.0f);
         }
     }
 }

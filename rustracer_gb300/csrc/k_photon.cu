@@ -351,15 +351,18 @@ __device__ __forceinline__ uint4 load_keys4(const uint32_t *__restrict__ keys, u
 // one warp rarely repeat, so merging lanes first costs more than it saves).
 __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                     uint32_t *__restrict__ counts) {
-    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    // eight keys per thread and pass, both 16-byte loads issued before the reductions
+    const uint64_t stride = 8ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t half = 4ull * gridDim.x * blockDim.x;
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
-        const uint4 k4 = load_keys4(keys, start + r * stride, n);
-        if (k4.x != kInvalidKey) atomicAdd(counts + k4.x, 1u);
-        if (k4.y != kInvalidKey) atomicAdd(counts + k4.y, 1u);
-        if (k4.z != kInvalidKey) atomicAdd(counts + k4.z, 1u);
-        if (k4.w != kInvalidKey) atomicAdd(counts + k4.w, 1u);
+        const uint4 a = load_keys4(keys, start + r * stride, n);
+        const uint4 b = load_keys4(keys, start + r * stride + half, n);
+        const uint32_t kk[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (kk[j] != kInvalidKey) atomicAdd(counts + kk[j], 1u);
     }
 }
 
@@ -368,20 +371,23 @@ __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                       const uint2 *__restrict__ meta, uint32_t *__restrict__ cursor,
                                                       uint32_t *__restrict__ order) {
-    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    // eight keys per thread and pass: loads, then all atomics and meta reads, then the stores
+    const uint64_t stride = 8ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t half = 4ull * gridDim.x * blockDim.x;
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
-        const uint64_t s0 = start + r * stride;
-        const uint4 k4 = load_keys4(keys, s0, n);
-        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-        uint32_t pos[4];
+        const uint64_t s0 = start + r * stride, s1 = s0 + half;
+        const uint4 a = load_keys4(keys, s0, n);
+        const uint4 b = load_keys4(keys, s1, n);
+        const uint32_t kk[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t pos[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 8; ++j)
             if (kk[j] != kInvalidKey) pos[j] = atomicAdd(cursor + kk[j], 1u) + __ldg(&meta[kk[j]].x);
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)(s0 + j);
+        for (int j = 0; j < 8; ++j)
+            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)((j < 4 ? s0 : s1) + (j & 3));
     }
 }
 
@@ -588,32 +594,42 @@ __device__ __forceinline__ void sort_cell_regs(uint32_t *__restrict__ order, uin
 __global__ void __launch_bounds__(256) multi_cells_kernel(const uint2 *__restrict__ meta, uint32_t n_cells,
                                                           uint32_t *__restrict__ list, uint32_t *__restrict__ n_list,
                                                           bool vec) {
+    // four cells per thread and pass (two 16-byte meta loads in flight)
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t n_pairs = (n_cells + 1u) / 2u;
+    const uint32_t n_quads = (n_cells + 3u) / 4u;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n_pairs + stride - 1) / stride;
+    const uint32_t rounds = (n_quads + stride - 1) / stride;
     for (uint32_t r = 0; r < rounds; ++r) {
-        const uint32_t pr = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const uint32_t c0 = 2u * pr;
-        uint32_t n0 = 0, n1 = 0;
-        if (vec && c0 + 1u < n_cells) {
-            const uint4 m = __ldg(reinterpret_cast<const uint4 *>(meta + c0));
-            n0 = m.y;
-            n1 = m.w;
+        const uint32_t c0 = 4u * (r * stride + blockIdx.x * blockDim.x + threadIdx.x);
+        uint32_t cnt[4] = {0u, 0u, 0u, 0u};
+        if (vec && c0 + 3u < n_cells) {
+            const uint4 m0 = __ldg(reinterpret_cast<const uint4 *>(meta + c0));
+            const uint4 m1 = __ldg(reinterpret_cast<const uint4 *>(meta + c0 + 2u));
+            cnt[0] = m0.y;
+            cnt[1] = m0.w;
+            cnt[2] = m1.y;
+            cnt[3] = m1.w;
         } else {
-            if (c0 < n_cells) n0 = __ldg(&meta[c0].y);
-            if (c0 + 1u < n_cells) n1 = __ldg(&meta[c0 + 1u].y);
+#pragma unroll
+            for (uint32_t j = 0; j < 4u; ++j)
+                if (c0 + j < n_cells) cnt[j] = __ldg(&meta[c0 + j].y);
         }
-        const bool w0 = n0 > 1u, w1 = n1 > 1u;
-        const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, w0), m1 = __ballot_sync(0xFFFFFFFFu, w1);
-        const uint32_t tot = __popc(m0) + __popc(m1);
+        uint32_t masks[4], tot = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 4u; ++j) {
+            masks[j] = __ballot_sync(0xFFFFFFFFu, cnt[j] > 1u);
+            tot += __popc(masks[j]);
+        }
         if (tot == 0u) continue;
         uint32_t base = 0;
         if (lane == 0u) base = atomicAdd(n_list, tot);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         const uint32_t lt = lanemask_lt();
-        if (w0) list[base + __popc(m0 & lt)] = c0;
-        if (w1) list[base + __popc(m0) + __popc(m1 & lt)] = c0 + 1u;
+#pragma unroll
+        for (uint32_t j = 0; j < 4u; ++j) {
+            if (cnt[j] > 1u) list[base + __popc(masks[j] & lt)] = c0 + j;
+            base += __popc(masks[j]);
+        }
     }
 }
 
@@ -652,37 +668,75 @@ __global__ void __launch_bounds__(kOrderWarps * 32) order_kernel(const uint2 *__
     }
 }
 
-// sorted[i] = photons[order[i]] for i < total; two photons per thread, all eight 16-byte loads
-// issued before the stores.
+struct Photon8 {
+    float v[16];
+};
+
+// 64 bytes as two 32-byte accesses (the records are 64-byte aligned when `wide`).
+__device__ __forceinline__ void load_photon_wide(const float4 *src, Photon8 &p) {
+    const float *f = reinterpret_cast<const float *>(src);
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(p.v[0]), "=f"(p.v[1]), "=f"(p.v[2]), "=f"(p.v[3]), "=f"(p.v[4]), "=f"(p.v[5]), "=f"(p.v[6]),
+                   "=f"(p.v[7])
+                 : "l"(f));
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(p.v[8]), "=f"(p.v[9]), "=f"(p.v[10]), "=f"(p.v[11]), "=f"(p.v[12]), "=f"(p.v[13]),
+                   "=f"(p.v[14]), "=f"(p.v[15])
+                 : "l"(f + 8));
+}
+
+__device__ __forceinline__ void store_photon_wide(float4 *dst, const Photon8 &p) {
+    float *f = reinterpret_cast<float *>(dst);
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(f), "f"(p.v[0]), "f"(p.v[1]), "f"(p.v[2]),
+                 "f"(p.v[3]), "f"(p.v[4]), "f"(p.v[5]), "f"(p.v[6]), "f"(p.v[7])
+                 : "memory");
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(f + 8), "f"(p.v[8]), "f"(p.v[9]),
+                 "f"(p.v[10]), "f"(p.v[11]), "f"(p.v[12]), "f"(p.v[13]), "f"(p.v[14]), "f"(p.v[15])
+                 : "memory");
+}
+
+// sorted[i] = photons[order[i]] for i < total, two photons per thread with both records loaded
+// before the stores; 32-byte accesses when both buffers are 32-byte aligned (`wide`).  sorted_pos,
+// when given, gets each photon's first float4.
 __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__restrict__ photons,
                                                             const uint32_t *__restrict__ order,
                                                             const uint32_t *__restrict__ total, uint64_t cap,
-                                                            float4 *__restrict__ sorted) {
+                                                            float4 *__restrict__ sorted,
+                                                            float4 *__restrict__ sorted_pos, bool wide) {
     const uint64_t n = min((uint64_t)__ldg(total), cap);
-    const uint64_t stride = 2ull * gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint64_t i2 = i + (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += 2 * step) {
+        const uint64_t i2 = i + step;
+        const bool two = i2 < n;
         const float4 *s0 = photons + 4ull * __ldg(order + i);
-        const float4 a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + 2), d = __ldg(s0 + 3);
-        float4 e = a, f = b, g = c, h = d;
-        if (i2 < n) {
-            const float4 *s1 = photons + 4ull * __ldg(order + i2);
-            e = __ldg(s1);
-            f = __ldg(s1 + 1);
-            g = __ldg(s1 + 2);
-            h = __ldg(s1 + 3);
-        }
-        float4 *d0 = sorted + 4ull * i;
-        d0[0] = a;
-        d0[1] = b;
-        d0[2] = c;
-        d0[3] = d;
-        if (i2 < n) {
-            float4 *d1 = sorted + 4ull * i2;
-            d1[0] = e;
-            d1[1] = f;
-            d1[2] = g;
-            d1[3] = h;
+        const float4 *s1 = photons + 4ull * __ldg(order + (two ? i2 : i));
+        if (wide) {
+            Photon8 a, b;
+            load_photon_wide(s0, a);
+            load_photon_wide(s1, b);
+            store_photon_wide(sorted + 4ull * i, a);
+            if (sorted_pos) sorted_pos[i] = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+            if (two) {
+                store_photon_wide(sorted + 4ull * i2, b);
+                if (sorted_pos) sorted_pos[i2] = make_float4(b.v[0], b.v[1], b.v[2], b.v[3]);
+            }
+        } else {
+            const float4 a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + 2), d = __ldg(s0 + 3);
+            const float4 e = __ldg(s1), f = __ldg(s1 + 1), g = __ldg(s1 + 2), h = __ldg(s1 + 3);
+            float4 *d0 = sorted + 4ull * i;
+            d0[0] = a;
+            d0[1] = b;
+            d0[2] = c;
+            d0[3] = d;
+            if (sorted_pos) sorted_pos[i] = a;
+            if (two) {
+                float4 *d1 = sorted + 4ull * i2;
+                d1[0] = e;
+                d1[1] = f;
+                d1[2] = g;
+                d1[3] = h;
+                if (sorted_pos) sorted_pos[i2] = e;
+            }
         }
     }
 }
@@ -700,25 +754,27 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
         return (unsigned)(b < 1 ? 1 : (b < cap ? b : cap));
     };
     if (n) {
-        count_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
+        count_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     // 16-byte vector access to counts / meta when the caller's buffers allow it
     const bool vec = (reinterpret_cast<uintptr_t>(g.counts) % 16u) == 0u && (reinterpret_cast<uintptr_t>(g.meta) % 16u) == 0u;
+    const bool wide = ((reinterpret_cast<uintptr_t>(g.photons) | reinterpret_cast<uintptr_t>(g.sorted)) % 32u) == 0u;
     const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
     scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
     scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
     scan_apply_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (n) {
-        scatter_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
+        scatter_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.meta, g.cursor, g.order);
         // The cells to order are listed in the cursor array (the cursors are spent after the scatter);
         // the list length is total[1].
         if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-        multi_cells_kernel<<<grid_for((C + 1) / 2, 256, 8), 256, 0, st>>>(g.meta, C, g.cursor, g.total + 1, vec);
+        multi_cells_kernel<<<grid_for((C + 3) / 4, 256, 8), 256, 0, st>>>(g.meta, C, g.cursor, g.total + 1, vec);
         order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(g.meta, g.cursor,
                                                                                                 g.total + 1, g.order);
-        photon_gather_kernel<<<grid_for((n + 1) / 2, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted);
+        photon_gather_kernel<<<grid_for((n + 1) / 2, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n, g.sorted,
+                                                                              g.sorted_pos, wide);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

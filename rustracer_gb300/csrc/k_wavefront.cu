@@ -511,25 +511,37 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                                         uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x +
                                                         (uint32_t)cz * gp.grid_x * gp.grid_y;
                                         uint2 m = __ldg(job.grid_meta + cell);
-                                        for (uint32_t k = 0; k < m.y && !done; ++k) {
-                                            if (budget == 0u) {
-                                                done = true;
-                                                break;
+                                        // Photons in groups of four: the group's positions are loaded
+                                        // together (from the compact position array when there is
+                                        // one), then tested in order with the budget and hit cap.
+                                        for (uint32_t k = 0; k < m.y && !done; k += 4u) {
+                                            float4 pos[4];
+#pragma unroll
+                                            for (uint32_t j = 0; j < 4u; ++j) {
+                                                uint64_t idx = (uint64_t)m.x + k + j;
+                                                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                                                pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx)
+                                                                        : __ldg(job.sorted_photons + 4ull * idx);
                                             }
-                                            budget -= 1u;
-                                            uint64_t idx = (uint64_t)m.x + k;
-                                            idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                                            const float4 *ph = job.sorted_photons + 4ull * idx;
-                                            f3 dd = xyz(__ldg(ph)) - hp;
-                                            float d2 = dot(dd, dd);
-                                            if (d2 < r2) {
-                                                f3 pw = xyz(__ldg(ph + 1));
-                                                f3 inc = xyz(__ldg(ph + 2));
-                                                ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
-                                                ph_hits += 1u;
-                                                if (ph_hits >= 64u) {
+#pragma unroll
+                                            for (uint32_t j = 0; j < 4u; ++j) {
+                                                if (done || k + j >= m.y) break;
+                                                if (budget == 0u) {
                                                     done = true;
                                                     break;
+                                                }
+                                                budget -= 1u;
+                                                f3 dd = xyz(pos[j]) - hp;
+                                                float d2 = dot(dd, dd);
+                                                if (d2 < r2) {
+                                                    uint64_t idx = (uint64_t)m.x + k + j;
+                                                    idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                                                    const float4 *ph = job.sorted_photons + 4ull * idx;
+                                                    f3 pw = xyz(__ldg(ph + 1));
+                                                    f3 inc = xyz(__ldg(ph + 2));
+                                                    ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
+                                                    ph_hits += 1u;
+                                                    if (ph_hits >= 64u) done = true;
                                                 }
                                             }
                                         }

@@ -16,6 +16,7 @@ struct DevJob {
     rt_image_params ip;
     rt_grid_params gp;
     const float4 *sorted_photons;  // 4 x float4 per photon
+    const float4 *sorted_pos;      // position of each sorted photon (its first float4), 16 B apart
     uint64_t sorted_count;
     const uint2 *grid_meta;        // (start, count) per cell
     uint32_t max_bounces, npix, base, spp;  // base: first path slot; spp = max(1, ip.spp)
@@ -105,6 +106,7 @@ struct GridBuffers {
     uint32_t *cursor;       // num_cells
     uint32_t *order;        // slot_count: slot indices in (cell, slot) order
     float4 *sorted;         // slot_count photons
+    float4 *sorted_pos;     // slot_count positions (the sorted photons' first float4), or null
     uint32_t *scan_partials;  // grid_scan_partials(num_cells) entries
     uint32_t *total;          // 4 entries: [0] binned photons, [1] cells holding two or more
 };

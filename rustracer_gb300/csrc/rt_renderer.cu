@@ -215,6 +215,7 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
     r->cfg.photon_radius = radius;
     const uint64_t S = r->photon_slots, C = r->gp.num_cells;
     if (r->d_photons.alloc(S * 64) != cudaSuccess || r->d_sorted.alloc(S * 64) != cudaSuccess ||
+        r->d_sorted_pos.alloc(S * 16) != cudaSuccess ||
         r->d_keys.alloc(S * 4) != cudaSuccess || r->d_order.alloc(S * 4) != cudaSuccess ||
         r->d_counts.alloc(C * 4) != cudaSuccess || r->d_cursor.alloc(C * 4) != cudaSuccess ||
         r->d_meta.alloc(C * 8) != cudaSuccess ||
@@ -226,6 +227,7 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
     }
     RT_CK(cudaMemsetAsync(r->d_photons.p, 0, S * 64, s));
     RT_CK(cudaMemsetAsync(r->d_sorted.p, 0, S * 64, s));
+    RT_CK(cudaMemsetAsync(r->d_sorted_pos.p, 0, S * 16, s));
     RT_CK(cudaMemsetAsync(r->d_keys.p, 0xFF, S * 4, s));
     RT_CK(cudaMemsetAsync(r->d_counts.p, 0, C * 4, s));
     RT_CK(cudaMemsetAsync(r->d_meta.p, 0, C * 8, s));
@@ -248,6 +250,7 @@ rt_renderer::~rt_renderer() {
 uint64_t rt_renderer::device_bytes() const {
     uint64_t n = d_lights.bytes + d_frame.bytes + d_pingpong.bytes + d_moments.bytes + d_gbuffer.bytes +
                  d_accum.bytes + d_output.bytes + d_photons.bytes + d_keys.bytes + d_order.bytes + d_sorted.bytes +
+                 d_sorted_pos.bytes +
                  d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
                  d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
     const rt::DevBuf *pb[10] = {&path.ro, &path.rd, &path.thr, &path.hit, &path.acc,
@@ -341,11 +344,11 @@ uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
 
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {
     // The allocations of create_on: frame buffers (5 x float4 + rgba8 per pixel), photon slots, keys,
-    // slot order and sorted photons, counts / cursor / meta per cell, scan partials, grid totals,
+    // slot order, sorted photons and their positions, counts / cursor / meta per cell, scan partials, grid totals,
     // counters, the one-entry job table and the renderer's own light buffer.
     const uint64_t npix = (uint64_t)c.width * c.height;
     const uint64_t S = photon_slots_of(c);
-    return npix * (5 * 16 + 4) + S * (64 + 64 + 4 + 4) + num_cells * 16 +
+    return npix * (5 * 16 + 4) + S * (64 + 64 + 16 + 4 + 4) + num_cells * 16 +
            (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + 16 + 64 + sizeof(rtd::DevJob) +
            sizeof(rt_light) * std::max<uint64_t>(n_lights, 1);
 }
@@ -445,6 +448,7 @@ rtd::DevJob make_job(const rt_renderer *r, uint32_t base) {
                                                     : 1.0f / (float)std::min(r->frames_since_reset, c.accumulate_frames));
     j.gp = r->gp;
     j.sorted_photons = r->d_sorted.as<float4>();
+    j.sorted_pos = r->d_sorted_pos.as<float4>();
     j.sorted_count = r->photon_slots;
     j.grid_meta = r->d_meta.as<uint2>();
     j.max_bounces = max_bounces(c);
@@ -601,6 +605,7 @@ static int build_grid(rt_renderer *r) {
     g.cursor = r->d_cursor.as<uint32_t>();
     g.order = r->d_order.as<uint32_t>();
     g.sorted = r->d_sorted.as<float4>();
+    g.sorted_pos = r->d_sorted_pos.as<float4>();
     g.scan_partials = r->d_partials.as<uint32_t>();
     g.total = r->d_total.as<uint32_t>();
     // Slots visited by the count/scatter dispatches of lib.rs:916,951,1026: floor(6P/256) groups of 256.
@@ -706,6 +711,29 @@ extern "C" int rt_set_light_marker(rt_renderer *r, const float marker[4], float 
 }
 
 extern "C" uint32_t rt_sample_count(const rt_renderer *r) { return r ? r->sample_counter : 0u; }
+
+extern "C" int rt_get_frame_state(const rt_renderer *r, uint32_t *sample_counter, uint32_t *frames_since_reset) {
+    if (int st = check_renderer(r, "rt_get_frame_state")) return st;
+    if (sample_counter) *sample_counter = r->sample_counter;
+    if (frames_since_reset) *frames_since_reset = r->frames_since_reset;
+    return RT_OK;
+}
+
+extern "C" int rt_restore_accumulation(rt_renderer *r, const float *rgba, uint64_t n_floats, uint32_t sample_counter,
+                                       uint32_t frames_since_reset) {
+    if (int st = check_renderer(r, "rt_restore_accumulation")) return st;
+    const uint64_t n = (uint64_t)r->cfg.width * r->cfg.height * 4;
+    if (!rgba || n_floats != n) {
+        set_error("rt_restore_accumulation: need %llu floats (W * H * 4), got %llu", (unsigned long long)n,
+                  (unsigned long long)n_floats);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    RT_CK(cudaMemcpyAsync(r->d_accum.p, rgba, n * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+    RT_CK(cudaStreamSynchronize(r->stream));  // the caller's buffer is only read during the call
+    r->sample_counter = sample_counter;
+    r->frames_since_reset = frames_since_reset;
+    return RT_OK;
+}
 
 extern "C" int rt_synchronize(rt_renderer *r) {
     if (int st = check_renderer(r, "rt_synchronize")) return st;
@@ -936,6 +964,7 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     g.cursor = cur.as<uint32_t>();
     g.order = order.as<uint32_t>();
     g.sorted = srt.as<float4>();
+    g.sorted_pos = nullptr;
     g.scan_partials = part.as<uint32_t>();
     g.total = tot.as<uint32_t>();
     RT_CK(rtd::launch_grid_build(g, 0));

@@ -210,6 +210,39 @@ class Renderer:
     def sample_count(self) -> int:
         return int(self._lib.rt_sample_count(self._h))
 
+    def frame_state(self) -> tuple[int, int]:
+        """(sample_counter, frames accumulated since the last reset)."""
+        a, b = C.c_uint32(), C.c_uint32()
+        A.check("rt_get_frame_state", self._lib.rt_get_frame_state(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def checkpoint(self, path) -> None:
+        """Writes the accumulation as raw little-endian f32 RGBA (render_headless.rs's raw dump) to
+        `path` and the frame counters to `path` + ".json"."""
+        import json
+        from pathlib import Path
+
+        acc = self.read_accumulation()
+        sc, fr = self.frame_state()
+        c = self.config
+        Path(path).write_bytes(acc.astype("<f4").tobytes())
+        Path(str(path) + ".json").write_text(json.dumps(
+            {"width": c.width, "height": c.height, "sample_counter": sc, "frames_since_reset": fr}))
+
+    def resume(self, path) -> None:
+        """Restores a checkpoint written by checkpoint() (same configuration, scene and camera)."""
+        import json
+        from pathlib import Path
+
+        meta = json.loads(Path(str(path) + ".json").read_text())
+        c = self.config
+        if (meta["width"], meta["height"]) != (c.width, c.height):
+            raise ValueError(f"checkpoint is {meta['width']}x{meta['height']}, the renderer {c.width}x{c.height}")
+        acc = np.frombuffer(Path(path).read_bytes(), dtype="<f4").astype(np.float32)
+        A.check("rt_restore_accumulation", self._lib.rt_restore_accumulation(
+            self._h, acc.ctypes.data_as(C.POINTER(C.c_float)), acc.size, meta["sample_counter"],
+            meta["frames_since_reset"]))
+
     def synchronize(self) -> None:
         A.check("rt_synchronize", self._lib.rt_synchronize(self._h))
 
