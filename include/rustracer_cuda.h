@@ -566,6 +566,11 @@ const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count);
 const uint32_t *rt_bvh_prims(const rt_bvh *b, uint64_t *count);
 void rt_bvh_destroy(rt_bvh *b);
 
+/* PNG scanline unfiltering for the glTF ingest (the reference decodes images through the `gltf` /
+ * `image` crates, rustracer-core/src/loader.rs:36-100): h rows of 1 + stride bytes (filter type
+ * first) in, h * stride unfiltered bytes out; bpp = bytes per pixel. */
+int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride, uint32_t bpp, uint8_t *out);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -54,8 +54,6 @@ __device__ __forceinline__ uint32_t slot_key(const rt_grid_params &gp, f3 pos, f
 
 }  // namespace
 
-constexpr int kTraceBlock = 128;
-
 // The photon's origin, direction and power as emitted from a light picked uniformly
 // (photon_trace.wgsl:91-190); false when no photon leaves (no lights, unknown kind).
 __device__ bool photon_emit(const PhotonTraceParams &p, uint32_t photon_index, Rng &rng, f3 &origin, f3 &dir,
@@ -244,13 +242,14 @@ __global__ void __launch_bounds__(128) ph_shade_kernel(const __grid_constant__ P
         if (item < n) {
             slot = q[item];
             const float2 h = w.hit[slot];
+            const float4 d = w.rd[slot];
+            const uint32_t photon_index = __float_as_uint(d.w);
             if (h.x < kInf) {
-                const float4 o = w.ro[slot], d = w.rd[slot], pw = w.pw[slot];
+                const float4 o = w.ro[slot], pw = w.pw[slot];
                 Rng rng;
                 rng.state = __float_as_uint(o.w);
                 f3 origin = xyz(o), dir = xyz(d), power = xyz(pw);
-                live = photon_bounce(p, __float_as_uint(d.w), iter, h.x, __float_as_uint(h.y), rng, origin, dir,
-                                     power) && !last;
+                live = photon_bounce(p, photon_index, iter, h.x, __float_as_uint(h.y), rng, origin, dir, power) && !last;
                 if (live) {
                     w.ro[slot] = make_float4(origin.x, origin.y, origin.z, __uint_as_float(rng.state));
                     w.rd[slot] = make_float4(dir.x, dir.y, dir.z, d.w);
@@ -572,10 +571,10 @@ __device__ __forceinline__ void warp_sort_regs(uint32_t (&v)[R], uint32_t lane) 
     }
 }
 
-// Sorts the cell's `count` (<= 32 R) slot indices order[start ..] in place.
+// Sorts the cell's `count` (<= 32 R) slot indices order[start ..], in place or (out != null) into out.
 template <int R>
 __device__ __forceinline__ void sort_cell_regs(uint32_t *__restrict__ order, uint32_t start, uint32_t count,
-                                               uint32_t lane) {
+                                               uint32_t lane, uint32_t *out = nullptr) {
     uint32_t v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -586,7 +585,10 @@ __device__ __forceinline__ void sort_cell_regs(uint32_t *__restrict__ order, uin
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const uint32_t e = lane * R + r;
-        if (e < count) order[start + e] = v[r];
+        if (e < count) {
+            if (out) out[e] = v[r];
+            else order[start + e] = v[r];
+        }
     }
 }
 
@@ -741,11 +743,110 @@ __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__rest
     }
 }
 
+// ---- grid build with per-slot ranks ---------------------------------------------------------------
+// Histogram with ranks: counts[key] += 1 and rank[slot] = the count found before the add (the slot's
+// position within its cell, in atomic order).
+__global__ void __launch_bounds__(256) count_rank_kernel(const uint32_t *__restrict__ keys, uint64_t n,
+                                                         uint32_t *__restrict__ counts, uint32_t *__restrict__ rank) {
+    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t rounds = (n + stride - 1) / stride;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const uint64_t s0 = start + r * stride;
+        const uint4 k4 = load_keys4(keys, s0, n);
+        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+        uint32_t rk[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) rk[j] = atomicAdd(counts + kk[j], 1u);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) rank[s0 + j] = rk[j];
+    }
+}
+
+// scan_apply plus the list of occupied cells (count >= 1), appended with one atomic per warp.
+__global__ void __launch_bounds__(kScanThreads) scan_apply_list_kernel(const uint32_t *__restrict__ counts, uint32_t n,
+                                                                       const uint32_t *__restrict__ partials,
+                                                                       uint2 *__restrict__ meta, bool vec,
+                                                                       uint32_t *__restrict__ list,
+                                                                       uint32_t *__restrict__ n_list) {
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    if (vec && base + kScanItems <= n) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(counts + base));
+        const uint4 b = __ldg(reinterpret_cast<const uint4 *>(counts + base + 4));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? __ldg(counts + base + i) : 0u;
+    }
+    uint32_t local = 0, occ = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) {
+        local += v[i];
+        occ += v[i] ? 1u : 0u;
+    }
+    uint32_t ex = block_exclusive_scan(local, warp_sums, nullptr) + __ldg(partials + blockIdx.x);
+    uint32_t st[kScanItems];
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) {
+        st[i] = ex;
+        ex += v[i];
+    }
+    if (vec && base + kScanItems <= n) {
+        uint4 *m4 = reinterpret_cast<uint4 *>(meta + base);
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; i += 2) m4[i / 2] = make_uint4(st[i], v[i], st[i + 1], v[i + 1]);
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i)
+            if (base + i < n) meta[base + i] = make_uint2(st[i], v[i]);
+    }
+    // warp-exclusive offsets of the occupied cells, one atomic per warp
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t x = occ;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    const uint32_t warp_total = __shfl_sync(0xFFFFFFFFu, x, 31);
+    uint32_t wbase = 0;
+    if (lane == 0u && warp_total) wbase = atomicAdd(n_list, warp_total);
+    wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0) + x - occ;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i)
+        if (v[i]) list[wbase++] = base + i;
+}
+
+// order[start[key] + rank[slot]] = slot: positions come from the ranks, no atomics.
+__global__ void __launch_bounds__(256) scatter_rank_kernel(const uint32_t *__restrict__ keys,
+                                                           const uint32_t *__restrict__ rank, uint64_t n,
+                                                           const uint2 *__restrict__ meta,
+                                                           uint32_t *__restrict__ order) {
+    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t rounds = (n + stride - 1) / stride;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const uint64_t s0 = start + r * stride;
+        const uint4 k4 = load_keys4(keys, s0, n);
+        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+        uint32_t pos[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) pos[j] = __ldg(&meta[kk[j]].x) + __ldg(rank + s0 + j);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)(s0 + j);
+    }
+}
+
 cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
     cudaError_t e;
     const uint32_t C = g.num_cells;
-    if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(g.cursor, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
     const uint64_t n = g.slot_count;
     const uint32_t sm = (uint32_t)num_sms();
     auto grid_for = [&](uint64_t items, uint32_t block, uint32_t per_sm) {
@@ -753,14 +854,35 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
         uint64_t cap = (uint64_t)sm * per_sm;
         return (unsigned)(b < 1 ? 1 : (b < cap ? b : cap));
     };
+    // 16-byte vector access to counts / meta, 32-byte photon copies, when the buffers allow it
+    const bool vec = (reinterpret_cast<uintptr_t>(g.counts) % 16u) == 0u && (reinterpret_cast<uintptr_t>(g.meta) % 16u) == 0u;
+    const bool wide = ((reinterpret_cast<uintptr_t>(g.photons) | reinterpret_cast<uintptr_t>(g.sorted)) % 32u) == 0u;
+    const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
+    if (g.rank) {
+        if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+        // The occupied cells are listed in the cursor array (no cursors are needed with ranks); the
+        // list length is total[1].
+        if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+        if (n) count_rank_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank);
+        scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
+        scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
+        scan_apply_list_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec, g.cursor,
+                                                               g.total + 1);
+        if (n) {
+            scatter_rank_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, g.rank, n, g.meta, g.order);
+            order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(
+                g.meta, g.cursor, g.total + 1, g.order);
+            photon_gather_kernel<<<grid_for((n + 1) / 2, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n,
+                                                                                  g.sorted, g.sorted_pos, wide);
+        }
+        return cudaGetLastError();
+    }
+    if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(g.cursor, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
     if (n) {
         count_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    // 16-byte vector access to counts / meta when the caller's buffers allow it
-    const bool vec = (reinterpret_cast<uintptr_t>(g.counts) % 16u) == 0u && (reinterpret_cast<uintptr_t>(g.meta) % 16u) == 0u;
-    const bool wide = ((reinterpret_cast<uintptr_t>(g.photons) | reinterpret_cast<uintptr_t>(g.sorted)) % 32u) == 0u;
-    const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
     scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
     scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
     scan_apply_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec);

@@ -1051,3 +1051,44 @@ extern "C" int rt_scene_default_camera(const rt_scene *s, rt_camera *out) {
     }
     return rt_camera_frame_scene(s, out);
 }
+
+// PNG scanline unfiltering (PNG specification, section 9: filter types None, Sub, Up, Average,
+// Paeth), for the glTF image decoder: `rows` holds h rows of 1 + stride bytes (filter byte first),
+// `out` receives h * stride bytes.  bpp = bytes per complete pixel (at least 1).
+extern "C" int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride, uint32_t bpp, uint8_t *out) {
+    rt::clear_error();
+    if ((!rows || !out) && h && stride) {
+        rt::set_error("rt_png_unfilter: null buffer");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    if (bpp == 0) bpp = 1;
+    for (uint32_t y = 0; y < h; ++y) {
+        const uint8_t f = rows[(size_t)y * (stride + 1)];
+        const uint8_t *in = rows + (size_t)y * (stride + 1) + 1;
+        uint8_t *o = out + (size_t)y * stride;
+        const uint8_t *up = y ? out + (size_t)(y - 1) * stride : nullptr;
+        for (uint32_t x = 0; x < stride; ++x) {
+            const int a = x >= bpp ? o[x - bpp] : 0;
+            const int b = up ? up[x] : 0;
+            const int c = (up && x >= bpp) ? up[x - bpp] : 0;
+            int pred = 0;
+            switch (f) {
+                case 0: pred = 0; break;
+                case 1: pred = a; break;
+                case 2: pred = b; break;
+                case 3: pred = (a + b) >> 1; break;
+                case 4: {
+                    const int p = a + b - c;
+                    const int pa = p > a ? p - a : a - p, pb = p > b ? p - b : b - p, pc = p > c ? p - c : c - p;
+                    pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                    break;
+                }
+                default:
+                    rt::set_error("rt_png_unfilter: unknown filter type %u in row %u", (unsigned)f, y);
+                    return RT_ERR_INVALID_ARGUMENT;
+            }
+            o[x] = (uint8_t)((in[x] + pred) & 0xFF);
+        }
+    }
+    return RT_OK;
+}

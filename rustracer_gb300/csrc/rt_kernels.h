@@ -108,7 +108,11 @@ struct GridBuffers {
     float4 *sorted;         // slot_count photons
     float4 *sorted_pos;     // slot_count positions (the sorted photons' first float4), or null
     uint32_t *scan_partials;  // grid_scan_partials(num_cells) entries
-    uint32_t *total;          // 4 entries: [0] binned photons, [1] cells holding two or more
+    uint32_t *total;          // 4 entries: [0] binned photons, [1] listed cells
+    // Optional per-slot rank within its cell (null: count and an atomic scatter, then a pass that
+    // lists the multi-photon cells).  With ranks the count pass records them, the scatter needs no
+    // atomics and the scan lists the occupied cells.
+    uint32_t *rank;
 };
 uint32_t grid_scan_partials(uint32_t num_cells);
 cudaError_t launch_photon_keys(const float4 *photons, uint64_t slot_count, const rt_grid_params &gp, uint32_t *keys,

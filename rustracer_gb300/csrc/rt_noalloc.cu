@@ -97,6 +97,7 @@ extern "C" int rt_stage_photon_grid_noalloc(const rt_photon *d_photons, const rt
     g.order = reinterpret_cast<uint32_t *>(b + kOrderOff);
     g.sorted = reinterpret_cast<float4 *>(d_sorted);
     g.sorted_pos = nullptr;
+    g.rank = nullptr;  // the scratch holds no rank array: count, atomic scatter, multi-photon cell pass
     g.scan_partials = reinterpret_cast<uint32_t *>(b + kPartialsOff);
     g.total = reinterpret_cast<uint32_t *>(b + kTotalOff);
     if ((e = rtd::launch_photon_keys(g.photons, g.slot_count, *gp, keys, st)) != cudaSuccess ||

@@ -215,7 +215,7 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
     r->cfg.photon_radius = radius;
     const uint64_t S = r->photon_slots, C = r->gp.num_cells;
     if (r->d_photons.alloc(S * 64) != cudaSuccess || r->d_sorted.alloc(S * 64) != cudaSuccess ||
-        r->d_sorted_pos.alloc(S * 16) != cudaSuccess ||
+        r->d_sorted_pos.alloc(S * 16) != cudaSuccess || r->d_rank.alloc(S * 4) != cudaSuccess ||
         r->d_keys.alloc(S * 4) != cudaSuccess || r->d_order.alloc(S * 4) != cudaSuccess ||
         r->d_counts.alloc(C * 4) != cudaSuccess || r->d_cursor.alloc(C * 4) != cudaSuccess ||
         r->d_meta.alloc(C * 8) != cudaSuccess ||
@@ -250,7 +250,7 @@ rt_renderer::~rt_renderer() {
 uint64_t rt_renderer::device_bytes() const {
     uint64_t n = d_lights.bytes + d_frame.bytes + d_pingpong.bytes + d_moments.bytes + d_gbuffer.bytes +
                  d_accum.bytes + d_output.bytes + d_photons.bytes + d_keys.bytes + d_order.bytes + d_sorted.bytes +
-                 d_sorted_pos.bytes +
+                 d_sorted_pos.bytes + d_rank.bytes +
                  d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
                  d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
     const rt::DevBuf *pb[10] = {&path.ro, &path.rd, &path.thr, &path.hit, &path.acc,
@@ -344,11 +344,11 @@ uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
 
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {
     // The allocations of create_on: frame buffers (5 x float4 + rgba8 per pixel), photon slots, keys,
-    // slot order, sorted photons and their positions, counts / cursor / meta per cell, scan partials, grid totals,
+    // ranks, slot order, sorted photons and their positions, counts / cursor / meta per cell, scan partials, grid totals,
     // counters, the one-entry job table and the renderer's own light buffer.
     const uint64_t npix = (uint64_t)c.width * c.height;
     const uint64_t S = photon_slots_of(c);
-    return npix * (5 * 16 + 4) + S * (64 + 64 + 16 + 4 + 4) + num_cells * 16 +
+    return npix * (5 * 16 + 4) + S * (64 + 64 + 16 + 4 + 4 + 4) + num_cells * 16 +
            (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + 16 + 64 + sizeof(rtd::DevJob) +
            sizeof(rt_light) * std::max<uint64_t>(n_lights, 1);
 }
@@ -595,6 +595,13 @@ extern "C" int rt_reset_accumulation(rt_renderer *r, int hard) {
     return RT_OK;
 }
 
+// Slots visited by the count/scatter dispatches of lib.rs:916,951,1026: floor(6P/256) groups of 256.
+static uint64_t counted_slots(const rt_renderer *r) {
+    const uint32_t P = std::max(r->cfg.photon_count, 1u);
+    const uint64_t dispatched = (uint64_t)std::max((uint32_t)(P * RT_MAX_BOUNCES) / 256u, 1u) * 256u;
+    return std::min<uint64_t>(dispatched, r->photon_slots);
+}
+
 static int build_grid(rt_renderer *r) {
     rtd::GridBuffers g;
     g.photons = r->d_photons.as<float4>();
@@ -608,10 +615,8 @@ static int build_grid(rt_renderer *r) {
     g.sorted_pos = r->d_sorted_pos.as<float4>();
     g.scan_partials = r->d_partials.as<uint32_t>();
     g.total = r->d_total.as<uint32_t>();
-    // Slots visited by the count/scatter dispatches of lib.rs:916,951,1026: floor(6P/256) groups of 256.
-    const uint32_t P = std::max(r->cfg.photon_count, 1u);
-    uint64_t dispatched = (uint64_t)std::max((uint32_t)(P * RT_MAX_BOUNCES) / 256u, 1u) * 256u;
-    g.slot_count = std::min<uint64_t>(dispatched, r->photon_slots);
+    g.rank = r->d_rank.as<uint32_t>();
+    g.slot_count = counted_slots(r);
     RT_CK(rtd::launch_grid_build(g, r->stream));
     return RT_OK;
 }
@@ -940,9 +945,10 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     }
     const rt_grid_params gp = *gpp;
     const uint64_t S = gp.photon_slots, C = gp.num_cells;
-    DevBuf ph, keys, order, srt, cnt, cur, mt, part, tot;
+    DevBuf ph, keys, rank, order, srt, cnt, cur, mt, part, tot;
     RT_CK(ph.alloc(S * 64));
     RT_CK(keys.alloc(S * 4));
+    RT_CK(rank.alloc(S * 4));
     RT_CK(order.alloc(S * 4));
     RT_CK(srt.alloc(S * 64));
     RT_CK(cnt.alloc(C * 4));
@@ -967,6 +973,7 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     g.sorted_pos = nullptr;
     g.scan_partials = part.as<uint32_t>();
     g.total = tot.as<uint32_t>();
+    g.rank = rank.as<uint32_t>();
     RT_CK(rtd::launch_grid_build(g, 0));
     RT_CK(cudaMemcpy(counts, cnt.p, C * 4, cudaMemcpyDeviceToHost));
     RT_CK(cudaMemcpy(meta, mt.p, C * 8, cudaMemcpyDeviceToHost));

@@ -203,8 +203,8 @@ struct rt_renderer {
     rt::JobTable jobs;
     rtd::WaveTuning tuning = rtd::default_tuning();  // solo frames
     int num_sms = 1;
-    rt::DevBuf d_photons, d_keys, d_order, d_sorted, d_sorted_pos, d_counts, d_meta, d_cursor, d_partials, d_total,
-        d_counters;
+    rt::DevBuf d_photons, d_keys, d_rank, d_order, d_sorted, d_sorted_pos, d_counts, d_meta, d_cursor, d_partials,
+        d_total, d_counters;
     uint64_t photon_slots = 1;
     bool photon_buffers = false;
     uint32_t sample_counter = 0, frames_since_reset = 0;

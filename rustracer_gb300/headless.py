@@ -4,10 +4,11 @@
     python -m rustracer_gb300.headless <scene> [frames] [out.png] [denoise] [app_like] [photons] [spp]
         [accum] [w] [h] [debug_view] [zoom] [yaw] [pitch] [raw_save] [--checkpoint P] [--resume P]
 
-<scene> is a procedural scene: `cornell` (the 555-unit Cornell box) or `icosphere[:level[:seed]]`
-(the displaced icosphere room); glTF files are not read by this backend.  Pass 1 for the boolean
-slots.  As in the reference: app_like means spp 4 and a 32-frame accumulation; the camera frames the
-scene (Camera::frame_scene) and is then zoomed / orbited; photon maps use 50,000 photons; the PNG is
+<scene> is a glTF / GLB file (read by rustracer_gb300.gltf, with a sibling scene.toml applied as the
+reference does) or a procedural scene: `cornell` (the 555-unit Cornell box) or
+`icosphere[:level[:seed]]` (the displaced icosphere room).  Pass 1 for the boolean slots.  As in the
+reference: app_like means spp 4 and a 32-frame accumulation; the camera frames the scene
+(Camera::frame_scene) and is then zoomed / orbited; photon maps use 50,000 photons; the PNG is
 the CPU Reinhard + gamma 2.2 of the accumulation (examples/common/mod.rs:37-47) and raw_save writes
 the accumulation as raw f32 RGBA to <out>.bin instead.  --checkpoint writes the accumulation and
 frame counters after the run, --resume continues a checkpointed run.
@@ -27,6 +28,10 @@ from .scene import Scene
 
 
 def make_scene(spec: str) -> Scene:
+    if spec.lower().endswith((".gltf", ".glb")):
+        from .gltf import load_gltf
+
+        return load_gltf(spec)
     name, *rest = spec.split(":")
     if name == "cornell":
         return Scene.cornell555()
@@ -34,7 +39,7 @@ def make_scene(spec: str) -> Scene:
         level = int(rest[0]) if rest else 8
         seed = int(rest[1]) if len(rest) > 1 else 0
         return Scene.icosphere_room(level, seed)
-    raise SystemExit(f"unknown scene {spec!r}: use cornell or icosphere[:level[:seed]] (glTF is not read here)")
+    raise SystemExit(f"unknown scene {spec!r}: use a .gltf / .glb file, cornell or icosphere[:level[:seed]]")
 
 
 def reinhard_png_bytes(acc: np.ndarray) -> np.ndarray:

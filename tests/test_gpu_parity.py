@@ -182,3 +182,27 @@ def test_photon_map_and_denoise_cornell(gpu, orc):
         o.record_frame()
     f = match_frac(r.read_accumulation(), o.accum)
     assert f >= FRAC, f
+
+
+def test_second_rebuild_counts_photons_left_from_the_first(gpu, orc):
+    """The histogram is taken inside the photon pass; slots the second pass does not write keep the
+    first pass's photons (the reference never clears the slot buffer) and must still be counted."""
+    scene = rt.Scene.cornell555()
+    cfg = rt.RenderConfig(width=16, height=16, spp=1, enable_photon_map=True, photon_count=4096 + 100,
+                          photon_scale=500.0)
+    r = rt.Renderer(scene, cfg)
+    r.rebuild_photons()
+    first = r.read_photons()
+    # a dimmer, moved light: different paths, so some slots of the first pass are not rewritten
+    r.update_lights([rt.point_light((278.0, 500.0, 278.0), (1.0, 1.0, 1.0), 0.4)])
+    r.rebuild_photons()
+    ph = r.read_photons()
+    stale = (first.view(np.uint8).reshape(len(first), -1) == ph.view(np.uint8).reshape(len(ph), -1)).all(1)
+    assert stale.sum() > 0 and (~stale).sum() > 0
+    counts, meta = r.read_photon_grid()
+    o = oracle_for(orc, scene, cfg, scene.default_camera())
+    o.load_photons(ph)  # the oracle's count pass over the whole slot buffer
+    assert np.array_equal(counts, o.grid_counts)
+    assert np.array_equal(meta, o.grid_meta)
+    srt = r.read_sorted_photons()
+    assert np.array_equal(srt[:o.binned].view(np.uint8), o.sorted[:o.binned].view(np.uint8))
