@@ -300,11 +300,12 @@ def photon_denoise_stages(steps: int, warmup: int, peak: float) -> dict:
     gat_ms = st.ms_gather_sum / frames
     npix = cfg.width * cfg.height
     t_ms, g_ms = statistics.median(trace_ms), statistics.median(grid_ms)
-    # Compulsory bytes of this dataflow (the trace emits u32 keys): keys read by count and scatter
-    # (4 + 4 B/slot), (start, count) written and counts read twice by the scan (16 B/cell), slot
-    # order written by scatter and read/written by the per-cell order pass (4 + 8 B per binned
-    # photon), and the 64 B photon read + 64 B write of the final gather.
-    grid_bytes = 8.0 * slots + 16.0 * cells + (12.0 + 128.0 + 4.0) * binned
+    # Compulsory bytes of this dataflow (the photon pass emits u32 keys): keys read by the count and
+    # the scatter (4 + 4 B/slot); counts read twice by the scan and (start, count) written (16 B/cell);
+    # per binned photon the rank written by the count and read by the scatter (4 + 4), the slot order
+    # written by the scatter, read and written by the per-cell order pass and read by the gather
+    # (4 + 4 + 4 + 4), the 64 B photon read + 64 B write of the gather and its 16 B compact position.
+    grid_bytes = 8.0 * slots + 16.0 * cells + (8.0 + 16.0 + 128.0 + 16.0) * binned
     den_bytes = 2 * 64.0 * npix
     res_bytes = 52.0 * npix
     r.close()

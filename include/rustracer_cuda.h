@@ -565,6 +565,9 @@ int rt_bvh_build(const float *centroids, const float *bbox_min, const float *bbo
 const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count);
 const uint32_t *rt_bvh_prims(const rt_bvh *b, uint64_t *count);
 void rt_bvh_destroy(rt_bvh *b);
+/* Threads of the host BVH build (0, the default: one per hardware thread; 1: sequential).  The
+ * tree does not depend on it. */
+void rt_set_host_threads(uint32_t n);
 
 /* PNG scanline unfiltering for the glTF ingest (the reference decodes images through the `gltf` /
  * `image` crates, rustracer-core/src/loader.rs:36-100): h rows of 1 + stride bytes (filter type

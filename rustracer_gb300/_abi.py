@@ -222,6 +222,7 @@ _PROTOS: dict[str, tuple] = {
     "rt_renderer_footprint": (C.c_int, [P(RenderConfigC), vp, P(u64), P(u64)]),
     "rt_get_frame_state": (C.c_int, [vp, P(u32), P(u32)]),
     "rt_restore_accumulation": (C.c_int, [vp, P(C.c_float), u64, u32, u32]),
+    "rt_set_host_threads": (None, [u32]),
     "rt_png_unfilter": (C.c_int, [P(C.c_uint8), u32, u32, u32, P(C.c_uint8)]),
     "rt_batch_create": (C.c_int, [P(vp), u32, u32, P(vp)]),
     "rt_batch_destroy": (None, [vp]),

@@ -14,8 +14,10 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <atomic>
 #include <memory>
 #include <new>
+#include <thread>
 #include <unordered_map>
 
 #include "rt_internal.h"
@@ -65,6 +67,9 @@ inline float surface_area(const Aabb &b) {
 }
 inline float comp(const Vec3 &v, int axis) { return axis == 0 ? v.x : (axis == 1 ? v.y : v.z); }
 
+// Worker threads of the host BVH build (0: one per hardware thread).
+std::atomic<unsigned> g_host_threads{0};
+
 struct Builder {
     const std::vector<Vec3> &centroids;
     std::vector<Aabb> boxes;
@@ -72,6 +77,9 @@ struct Builder {
     std::vector<uint32_t> prims;
     static constexpr size_t kMaxLeaf = 4;
     static constexpr int kBins = 12;
+    // Subtrees with at least this many primitives near the top of the tree are built on their own
+    // thread; the result is identical to the sequential build (see build()).
+    static constexpr size_t kParallelMin = 8192;
 
     bool best_split(size_t start, size_t end, const Aabb &bb, int *axis_out, size_t *left_out) const {
         float bb_sa = surface_area(bb);
@@ -144,7 +152,11 @@ struct Builder {
         return false;
     }
 
-    uint32_t build(size_t start, size_t end) {
+    // Appends the subtree over prims[start, end) to `out` in post-order (children before parent) and
+    // returns its root's index in `out`.  With par_depth > 0 the left subtree is built on another
+    // thread into its own vector and both are appended in the sequential order afterwards, their
+    // child indices shifted: the nodes and the prim order equal those of the sequential build.
+    uint32_t build(size_t start, size_t end, std::vector<rt_bvh_node> &out, int par_depth) {
         size_t count = end - start;
         if (count == 0) return 0;
         Aabb bb = aabb_empty();
@@ -160,8 +172,8 @@ struct Builder {
             node.left_first = (uint32_t)start;
             node.right_child = 0;
             node.prim_count = (uint32_t)count;
-            nodes.push_back(node);
-            return (uint32_t)(nodes.size() - 1);
+            out.push_back(node);
+            return (uint32_t)(out.size() - 1);
         }
         size_t mid = start + left_count;
         const std::vector<Vec3> &cs = centroids;
@@ -172,13 +184,40 @@ struct Builder {
                              if (cb < ca) return false;
                              return a < b;
                          });
-        uint32_t left = build(start, mid);
-        uint32_t right = build(mid, end);
+        uint32_t left, right;
+        if (par_depth > 0 && count >= kParallelMin) {
+            std::vector<rt_bvh_node> lnodes, rnodes;
+            uint32_t lroot = 0;
+            std::thread t([&] { lroot = build(start, mid, lnodes, par_depth - 1); });
+            const uint32_t rroot = build(mid, end, rnodes, par_depth - 1);
+            t.join();
+            const uint32_t lbase = (uint32_t)out.size();
+            for (rt_bvh_node nd : lnodes) {
+                if (nd.prim_count == 0) {
+                    nd.left_first += lbase;
+                    nd.right_child += lbase;
+                }
+                out.push_back(nd);
+            }
+            const uint32_t rbase = (uint32_t)out.size();
+            for (rt_bvh_node nd : rnodes) {
+                if (nd.prim_count == 0) {
+                    nd.left_first += rbase;
+                    nd.right_child += rbase;
+                }
+                out.push_back(nd);
+            }
+            left = lbase + lroot;
+            right = rbase + rroot;
+        } else {
+            left = build(start, mid, out, 0);
+            right = build(mid, end, out, 0);
+        }
         node.left_first = left;
         node.right_child = right;
         node.prim_count = 0;
-        nodes.push_back(node);
-        return (uint32_t)(nodes.size() - 1);
+        out.push_back(node);
+        return (uint32_t)(out.size() - 1);
     }
 };
 
@@ -192,7 +231,11 @@ BVH build_bvh(const std::vector<Vec3> &centroids, const std::vector<Vec3> &bmin,
     b.prims.resize(n);
     for (size_t i = 0; i < n; ++i) b.prims[i] = (uint32_t)i;
     b.nodes.reserve(n > 0 ? 2 * n / 2 + 1 : 0);
-    b.build(0, n);
+    unsigned threads = g_host_threads.load();
+    if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+    int par_depth = 0;
+    while ((1u << par_depth) < threads && par_depth < 8) ++par_depth;
+    b.build(0, n, b.nodes, par_depth);
     // reverse_nodes (bvh.rs:322-335)
     size_t cnt = b.nodes.size();
     if (cnt > 1) {
@@ -1092,3 +1135,5 @@ extern "C" int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride,
     }
     return RT_OK;
 }
+
+extern "C" void rt_set_host_threads(uint32_t n) { g_host_threads.store(n); }

@@ -156,3 +156,21 @@ def test_oracle_traversal_matches_brute_force(lib, orc):
         assert t[k] == tb
         if t[k] < 1e38:
             assert prim[k] == ib or t[k] == brute_force(tris[[prim[k]]], o[k], d[k])[0]
+
+
+def test_threaded_build_equals_sequential_build():
+    """The host BVH build splits the top of the tree over threads; nodes and prim order are those of
+    the sequential build."""
+    from rustracer_gb300 import _abi as A
+    import rustracer_gb300 as rt
+
+    lib = A.load()
+    out = []
+    for threads in (1, 0, 3):
+        lib.rt_set_host_threads(threads)
+        s = rt.Scene.icosphere_room(level=5, seed=11, tex_size=8)
+        a = s.arrays()
+        out.append((a["bvh_nodes"].tobytes(), a["bvh_prims"].tobytes()))
+    lib.rt_set_host_threads(0)
+    assert out[0] == out[1] == out[2]
+    assert len(out[0][1]) // 4 >= 20 * 4 ** 5  # large enough for threaded subtrees (8192 prims each)
