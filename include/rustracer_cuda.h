@@ -565,6 +565,21 @@ int rt_bvh_build(const float *centroids, const float *bbox_min, const float *bbo
 const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count);
 const uint32_t *rt_bvh_prims(const rt_bvh *b, uint64_t *count);
 void rt_bvh_destroy(rt_bvh *b);
+/* BVH builders (no counterpart in the reference, which builds on the host only): RT_BVH_HOST_SAH is
+ * BVHBuilder::build (bvh.rs:135-336, the default); RT_BVH_GPU_LBVH builds a linear BVH on the GPU
+ * (Morton codes of the centroids, one primitive per leaf) in the same node layout, falling back to
+ * the host build when no device is visible or the tree is deeper than 62 levels (the traversal
+ * stack's bound).  The images are the same with either tree except where two triangles are hit at
+ * exactly the same distance.  Changing the builder of a finalized scene flattens it again at the
+ * next rt_scene_describe (descriptions taken before become invalid; renderers already created keep
+ * their own copies). */
+#define RT_BVH_HOST_SAH 0u
+#define RT_BVH_GPU_LBVH 1u
+int rt_scene_set_bvh_builder(rt_scene *s, uint32_t builder);
+uint32_t rt_scene_bvh_builder_used(const rt_scene *s);
+/* The GPU build on raw primitive boxes (n >= 2); *max_depth (optional) gets the tree's depth. */
+int rt_bvh_build_gpu(const float *centroids, const float *bbox_min, const float *bbox_max, uint64_t n,
+                     rt_bvh **out, uint32_t *max_depth);
 /* Threads of the host BVH build (0, the default: one per hardware thread; 1: sequential).  The
  * tree does not depend on it. */
 void rt_set_host_threads(uint32_t n);

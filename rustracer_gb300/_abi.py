@@ -30,6 +30,7 @@ GRID_MAX_DIM = 26
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE = 0, 1, 2, 3
 LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_AREA, LIGHT_ENVIRONMENT = 0, 1, 2, 3
 TEX_ALBEDO, TEX_MR, TEX_EMISSIVE, TEX_NORMAL = 0, 1, 2, 3
+BVH_HOST_SAH, BVH_GPU_LBVH = 0, 1
 NOALLOC_MAX_SLOTS = 1 << 20
 NOALLOC_MAX_CELLS = 1 << 18
 NOALLOC_SCRATCH_BYTES = 9438208
@@ -223,6 +224,9 @@ _PROTOS: dict[str, tuple] = {
     "rt_get_frame_state": (C.c_int, [vp, P(u32), P(u32)]),
     "rt_restore_accumulation": (C.c_int, [vp, P(C.c_float), u64, u32, u32]),
     "rt_set_host_threads": (None, [u32]),
+    "rt_scene_set_bvh_builder": (C.c_int, [vp, u32]),
+    "rt_scene_bvh_builder_used": (u32, [vp]),
+    "rt_bvh_build_gpu": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float), u64, P(vp), P(u32)]),
     "rt_png_unfilter": (C.c_int, [P(C.c_uint8), u32, u32, u32, P(C.c_uint8)]),
     "rt_batch_create": (C.c_int, [P(vp), u32, u32, P(vp)]),
     "rt_batch_destroy": (None, [vp]),

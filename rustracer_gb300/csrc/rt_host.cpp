@@ -690,7 +690,18 @@ extern "C" int rt_scene_finalize(rt_scene *s) {
             bmax.push_back(hi);
         }
     }
-    s->bvh = build_bvh(centroids, bmin, bmax);
+    s->bvh_builder_used = RT_BVH_HOST_SAH;
+    if (s->bvh_builder == RT_BVH_GPU_LBVH && ntri >= 2 && rt_device_count() > 0) {
+        static_assert(sizeof(Vec3) == 12, "Vec3 arrays are read as packed floats");
+        uint32_t depth = 0;
+        rt::BVH b;
+        // The traversal stack holds at most 63 pending nodes: deeper trees take the host build.
+        if (rtd::build_lbvh(&centroids[0].x, &bmin[0].x, &bmax[0].x, (uint32_t)ntri, b, &depth) == 0 && depth <= 62) {
+            s->bvh = std::move(b);
+            s->bvh_builder_used = RT_BVH_GPU_LBVH;
+        }
+    }
+    if (s->bvh_builder_used == RT_BVH_HOST_SAH) s->bvh = build_bvh(centroids, bmin, bmax);
     s->has_bounds = !(mn.x > mx.x);
     st3(s->bounds_min, s->has_bounds ? mn : Vec3{0, 0, 0});
     st3(s->bounds_max, s->has_bounds ? mx : Vec3{0, 0, 0});
@@ -1137,3 +1148,36 @@ extern "C" int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride,
 }
 
 extern "C" void rt_set_host_threads(uint32_t n) { g_host_threads.store(n); }
+
+extern "C" int rt_scene_set_bvh_builder(rt_scene *s, uint32_t builder) {
+    if (!s || builder > RT_BVH_GPU_LBVH) {
+        set_error("rt_scene_set_bvh_builder: need a scene and RT_BVH_HOST_SAH or RT_BVH_GPU_LBVH");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    if (s->finalized && s->bvh_builder != builder) s->finalized = false;  // rebuilt at the next describe
+    s->bvh_builder = builder;
+    return RT_OK;
+}
+
+extern "C" uint32_t rt_scene_bvh_builder_used(const rt_scene *s) { return s ? s->bvh_builder_used : 0u; }
+
+extern "C" int rt_bvh_build_gpu(const float *centroids, const float *bbox_min, const float *bbox_max, uint64_t n,
+                                rt_bvh **out, uint32_t *max_depth) {
+    rt::clear_error();
+    if (!out || n < 2 || n > 0x7FFFFFFFull || !centroids || !bbox_min || !bbox_max) {
+        set_error("rt_bvh_build_gpu: need 2 .. 2^31 - 1 primitives and their centroids and boxes");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    rt_bvh *b = new (std::nothrow) rt_bvh();
+    if (!b) {
+        set_error("rt_bvh_build_gpu: out of host memory");
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    if (rtd::build_lbvh(centroids, bbox_min, bbox_max, (uint32_t)n, b->b, max_depth) != 0) {
+        delete b;
+        set_error("rt_bvh_build_gpu: a CUDA call failed");
+        return RT_ERR_CUDA;
+    }
+    *out = b;
+    return RT_OK;
+}

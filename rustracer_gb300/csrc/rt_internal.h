@@ -72,6 +72,8 @@ struct rt_scene {
     std::vector<rt_material> materials;
     std::vector<rt_light> lights;
     rt::Texture tex[4];
+    // BVH builder of rt_scene_finalize: RT_BVH_HOST_SAH or RT_BVH_GPU_LBVH (and the one used).
+    uint32_t bvh_builder = 0, bvh_builder_used = 0;
     // Flattened state (rt_scene_finalize).
     bool finalized = false;
     std::vector<rt_triangle> triangles;
@@ -86,3 +88,10 @@ struct rt_scene {
 struct rt_bvh {
     rt::BVH b;
 };
+
+namespace rtd {
+// Linear BVH of n >= 2 primitives built on the GPU (k_bvh.cu), in the reference's node layout; 0 on
+// success (with the tree's depth), < 0 when n < 2 or a CUDA call failed.
+int build_lbvh(const float *centroids, const float *bmin, const float *bmax, uint32_t n, rt::BVH &out,
+               uint32_t *max_depth);
+}  // namespace rtd

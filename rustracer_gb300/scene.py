@@ -192,6 +192,14 @@ class Scene:
     def triangle_count(self) -> int:
         return int(A.load().rt_scene_triangle_count(self._h))
 
+    def set_bvh_builder(self, builder: int) -> None:
+        """A.BVH_HOST_SAH (the reference's builder, default) or A.BVH_GPU_LBVH; before finalizing."""
+        A.check("rt_scene_set_bvh_builder", A.load().rt_scene_set_bvh_builder(self._h, builder))
+        self._desc = None  # flattened again with the new tree at the next describe
+
+    def bvh_builder_used(self) -> int:
+        return int(A.load().rt_scene_bvh_builder_used(self._h))
+
     def default_camera(self) -> Camera:
         c = A.Camera()
         A.check("rt_scene_default_camera", A.load().rt_scene_default_camera(self._h, C.byref(c)))
