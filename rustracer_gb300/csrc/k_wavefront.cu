@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
                                                            uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
+    WarpLeaves &wl = reinterpret_cast<WarpLeaves *>(stack_smem + kStack * kBlock)[threadIdx.x >> 5];
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
     uint32_t *fetch = p.counts + 4 * iter + 2;
@@ -297,14 +298,17 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
             if (sc.cnode_count == 0u) {
                 p.hit[slot] = make_float2(kInf, 0.0f);
                 has = false;
+            } else {
+                warp_leaves_set_ray(wl, st);
             }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
-        for (uint32_t k = 0; k < steps && has; ++k) {
-            if (trav_step<false>(st, stk, (uint32_t)kBlock)) {
+        for (uint32_t k = 0; k < steps; ++k) {
+            if (trav_step_warp(st, has, false, stk, (uint32_t)kBlock, wl)) {
                 p.hit[slot] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
             }
+            if (!__any_sync(0xFFFFFFFFu, has)) break;
         }
     }
 }
@@ -655,6 +659,7 @@ __global__ void __launch_bounds__(kBlock) wf_shadow_kernel(const __grid_constant
                                                            uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
+    WarpLeaves &wl = reinterpret_cast<WarpLeaves *>(stack_smem + kStack * kBlock)[threadIdx.x >> 5];
     const uint32_t m = p.counts[4 * iter + 1];
     uint32_t *fetch = p.counts + 4 * iter + 3;
     WarpFeed feed;
@@ -677,16 +682,17 @@ __global__ void __launch_bounds__(kBlock) wf_shadow_kernel(const __grid_constant
             if (!has) {
                 st.t = kInf;
                 shadow_resolve(p, rec_i, st, limit);
+            } else {
+                warp_leaves_set_ray(wl, st);
             }
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
-        for (uint32_t k = 0; k < steps && has; ++k) {
-            const bool done = any_hit ? trav_step<true>(st, stk, (uint32_t)kBlock)
-                                      : trav_step<false>(st, stk, (uint32_t)kBlock);
-            if (done) {
+        for (uint32_t k = 0; k < steps; ++k) {
+            if (trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
                 shadow_resolve(p, rec_i, st, limit);
                 has = false;
             }
+            if (!__any_sync(0xFFFFFFFFu, has)) break;
         }
     }
 }
@@ -780,6 +786,11 @@ void pick(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
     }
 }
 
+// Dynamic shared memory of a traversal block: the lane-interleaved stacks, then one WarpLeaves per warp.
+size_t trav_smem_bytes(const WaveTuning &t) {
+    return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves);
+}
+
 void trav_kernels(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
     ext = shd = nullptr;
     pick<32, 64>(t, ext, shd);
@@ -796,10 +807,13 @@ void trav_kernels(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
 }  // namespace
 
 void prepare_wavefront_kernels() {
-    // Stacks above 48 KB per block (64 entries x 256 lanes) need the dynamic shared-memory opt-in.
-    const int bytes = 64 * 256 * (int)sizeof(uint32_t);
-    cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(wf_shadow_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    // Blocks above 48 KB of dynamic shared memory (64- and 48-entry stacks x 256 lanes) need the opt-in.
+    const int b64 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 64u});
+    const int b48 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 48u});
+    cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
+    cudaFuncSetAttribute(wf_shadow_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
+    cudaFuncSetAttribute(wf_extend_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
+    cudaFuncSetAttribute(wf_shadow_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
 }
 
 cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
@@ -808,7 +822,7 @@ cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items
     normalize_tuning(t, stack_need);
     TravKernel ext, shd;
     trav_kernels(t, ext, shd);
-    const size_t smem = (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t);
+    const size_t smem = trav_smem_bytes(t);
     const uint64_t blocks_needed = (max_items + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? (blocks_needed ? blocks_needed : 1u) : persistent);
@@ -832,7 +846,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     normalize_tuning(t, stack_need);
     TravKernel ext, shd;
     trav_kernels(t, ext, shd);
-    const size_t smem = (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t);
+    const size_t smem = trav_smem_bytes(t);
     const uint64_t blocks_needed = (slots + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);

@@ -364,6 +364,150 @@ __device__ __forceinline__ bool trav_step(TravState &st, uint32_t *stk, uint32_t
     return false;
 }
 
+// Warp-cooperative form of trav_step for the persistent traversal kernels.  Every lane of the warp
+// calls it together; `active` lanes advance their own traversal by one record exactly as trav_step
+// does, but the triangles of the record's hit leaves are tested by the whole warp: the leaf work of
+// all lanes is laid out as one list (lane order, left leaf before right leaf, triangles in leaf
+// order), cut into rounds of 32 tests, one per lane, and each lane then folds the results of its own
+// tests in list order with the reference's rule (a test wins when its t is strictly below the best so
+// far).  The result is trav_step's; only the lanes that do the arithmetic change.  With trav_step a
+// lane whose record holds four-triangle leaves tests them one after another while the rest of the
+// warp waits.
+//
+// `any` lanes stop at the first record whose leaves hold a triangle below st.t (the occlusion query);
+// st.t then holds the smallest such t of that record rather than the first.  WarpLeaves is per warp
+// and set_ray must have stored a lane's ray before its first step.
+struct WarpLeaves {
+    float4 ray[2][32];  // per lane: (ro, low half of tri_ord), (rd, high half of tri_ord)
+    uint32_t owner[32];
+    float t[32];
+    uint32_t prim[32];
+};
+
+__device__ __forceinline__ void warp_leaves_set_ray(WarpLeaves &w, const TravState &st) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long tp = (unsigned long long)st.tri_ord;
+    w.ray[0][lane] = make_float4(st.ro.x, st.ro.y, st.ro.z, __uint_as_float((uint32_t)tp));
+    w.ray[1][lane] = make_float4(st.rd.x, st.rd.y, st.rd.z, __uint_as_float((uint32_t)(tp >> 32)));
+}
+
+__device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
+                                               WarpLeaves &w) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool hl = false, hr = false;
+    float le = 0.0f, re = 0.0f;
+    uint32_t lref = 0u, lcnt = 0u, rref = 0u, rcnt = 0u;
+    if (active) {
+        const float4 *np = st.cnodes + 4ull * st.node;
+        const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        const f3 ro = st.ro, inv = st.inv;
+        const f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
+        const f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
+        le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
+        const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
+        re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
+        const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
+        hl = le <= lx && lx > 0.0f && le < st.t;
+        hr = re <= rx && rx > 0.0f && re < st.t;
+        lref = __float_as_uint(q0.w);
+        lcnt = __float_as_uint(q1.w);
+        rref = __float_as_uint(q2.w);
+        rcnt = __float_as_uint(q3.w);
+    }
+    const uint32_t nl = (hl && lcnt != 0u) ? lcnt : 0u;
+    const uint32_t n = nl + ((hr && rcnt != 0u) ? rcnt : 0u);
+    uint32_t incl = n;
+#pragma unroll
+    for (uint32_t d = 1u; d < 32u; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t excl = incl - n;
+    bool found = false;
+    for (uint32_t base = 0u; base < total; base += 32u) {
+        // This round tests list entries [base, base + 32); a lane owning some of them marks where its
+        // run starts, so every position finds its owner as the last start at or below it.
+        const uint32_t lo = excl > base ? excl : base;
+        const uint32_t hi = excl + n < base + 32u ? excl + n : base + 32u;
+        const bool mine = lo < hi;
+        if (mine) w.owner[lo - base] = lane;
+        const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, mine ? 1u << (lo - base) : 0u);
+        __syncwarp();
+        const uint32_t start = 31u - __clz((starts | 1u) & (0xFFFFFFFFu >> (31u - lane)));
+        const uint32_t o = w.owner[start];
+        const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, excl, o);
+        const uint32_t o_nl = __shfl_sync(0xFFFFFFFFu, nl, o);
+        const uint32_t o_lref = __shfl_sync(0xFFFFFFFFu, lref, o);
+        const uint32_t o_rref = __shfl_sync(0xFFFFFFFFu, rref, o);
+        float t = kInf;
+        uint32_t prim = 0u;
+        if (base + lane < total) {
+            const float4 r0 = w.ray[0][o], r1 = w.ray[1][o];
+            const float4 *tris = reinterpret_cast<const float4 *>(
+                ((unsigned long long)__float_as_uint(r1.w) << 32) | (unsigned long long)__float_as_uint(r0.w));
+            const uint32_t j = base + lane - o_excl;
+            const uint32_t tri = j < o_nl ? o_lref + j : o_rref + (j - o_nl);
+            const float4 *tp = tris + 3ull * tri;
+            const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+            const f3 ro = xyz(r0), rd = xyz(r1);
+            // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed, as in trav_step.
+            const f3 h3 = cross(rd, xyz(e2));
+            const float a = dot(xyz(e1), h3);
+            if (!(fabsf(a) < 1e-7f)) {
+                const float f = 1.0f / a;
+                const f3 sv = ro - xyz(v0);
+                const float u = f * dot(sv, h3);
+                if (!(u < 0.0f || u > 1.0f)) {
+                    const f3 q = cross(sv, xyz(e1));
+                    const float v = f * dot(rd, q);
+                    if (!(v < 0.0f || u + v > 1.0f)) {
+                        const float tt = f * dot(xyz(e2), q);
+                        if (tt > kEps) t = tt;
+                    }
+                }
+            }
+            prim = __float_as_uint(v0.w);
+        }
+        w.t[lane] = t;
+        w.prim[lane] = prim;
+        __syncwarp();
+        if (mine) {
+            for (uint32_t k = lo - base; k < hi - base; ++k) {
+                const float tk = w.t[k];
+                if (tk < st.t) {
+                    st.t = tk;
+                    st.prim = w.prim[k];
+                    found = true;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (!active) return false;
+    if (any && found) return true;
+    hl = hl && lcnt == 0u;
+    hr = hr && rcnt == 0u;
+    if (hl && hr) {
+        const bool left_first = le <= re;
+        const uint32_t far = left_first ? rref : lref;
+        st.node = left_first ? lref : rref;
+        if (st.sp < st.cap) {
+            stk[st.sp * stride] = far;
+            st.sp += 1u;
+        }
+    } else if (hl) {
+        st.node = lref;
+    } else if (hr) {
+        st.node = rref;
+    } else {
+        if (st.sp == 0u) return true;
+        st.sp -= 1u;
+        st.node = stk[st.sp * stride];
+    }
+    return false;
+}
+
 template <bool kAny>
 __device__ __forceinline__ Hit trace(const DevScene &s, f3 ro, f3 rd, float t_limit, uint32_t *stk,
                                      uint32_t stride) {
