@@ -11,6 +11,10 @@
 //   shadow     occlusion of each deferred NEE ray; a visible light adds its contribution
 //   finalize   sigma clamp and the frame / moments / gbuffer writes (gather.wgsl:548-593)
 //
+// extend and shadow run as one persistent traversal launch (`wf_trace_kernel`): the occlusion rays of
+// iteration i-1 ride with the closest-hit rays of iteration i, which need only shade(i-1) too.  The
+// photon pass uses the closest-hit-only form (`wf_extend_kernel`).
+//
 // One path slot per pixel: a pixel's samples run one after the other in its slot, with one RNG
 // stream, exactly as the reference's per-pixel loop.  Every pixel receives its contributions in the
 // reference's order except that a bounce's NEE term lands after that bounce's other terms; floating
@@ -654,42 +658,62 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
     store_acc(p, slot, A, acc1);
 }
 
+// trace: the occlusion rays of iteration `shd_iter` and the closest-hit rays of iteration `ext_iter` in
+// one persistent launch (either may be kNoIter).  Both depend only on the shade pass before them and
+// touch disjoint state (shadow records and accumulators / path rays and hits), so one launch carries
+// them with one tail instead of two.  Closest-hit rays come first in the work list: the longer rays
+// start early and the shorter occlusion rays fill the end.
+constexpr uint32_t kNoIter = 0xFFFFFFFFu;
+
 template <int kStack, int kBlock>
-__global__ void __launch_bounds__(kBlock) wf_shadow_kernel(const __grid_constant__ WaveParams p, uint32_t iter,
-                                                           uint32_t chunk, uint32_t steps) {
+__global__ void __launch_bounds__(kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
+                                                          uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
     WarpLeaves &wl = reinterpret_cast<WarpLeaves *>(stack_smem + kStack * kBlock)[threadIdx.x >> 5];
-    const uint32_t m = p.counts[4 * iter + 1];
-    uint32_t *fetch = p.counts + 4 * iter + 3;
+    const uint32_t n_ext = ext_iter != kNoIter ? p.counts[4 * ext_iter] : 0u;
+    const uint32_t n_shd = shd_iter != kNoIter ? p.counts[4 * shd_iter + 1] : 0u;
+    const uint32_t *q = p.queue[ext_iter & 1u];
+    uint32_t *fetch = ext_iter != kNoIter ? p.counts + 4 * ext_iter + 2 : p.counts + 4 * shd_iter + 3;
     WarpFeed feed;
     TravState st;
-    bool has = false, any_hit = true;
-    uint32_t rec_i = 0;
+    bool has = false, occlusion = false, any_hit = false;
+    uint32_t id = 0;  // path slot (closest hit) or shadow record (occlusion)
     float limit = 0.0f;
     for (;;) {
-        const uint32_t item = warp_take(feed, !has, m, fetch, chunk);
+        const uint32_t item = warp_take(feed, !has, n_ext + n_shd, fetch, chunk);
         if (item != 0xFFFFFFFFu) {
-            rec_i = item;
-            const float4 o = p.shadow[3ull * rec_i], d = p.shadow[3ull * rec_i + 1];
-            const DevScene &sc = p.jobs[__float_as_uint(p.shadow[3ull * rec_i + 2].w) >> 17].scene;
-            limit = o.w - 0.001f;
-            // Without cut-out materials the occlusion test may stop at the first triangle below the
-            // limit; with them the reference's closest-hit-then-alpha rule is kept.
-            any_hit = sc.any_hit_shadows != 0u;
-            st = trav_begin(sc, xyz(o), xyz(d), any_hit ? limit : kInf);
-            has = sc.cnode_count != 0u;
-            if (!has) {
-                st.t = kInf;
-                shadow_resolve(p, rec_i, st, limit);
+            occlusion = item >= n_ext;
+            if (!occlusion) {
+                id = q[item];
+                const float4 o = p.ro[id], d = p.rd[id];
+                const DevScene &sc = p.jobs[__float_as_uint(p.thr[id].w)].scene;
+                any_hit = false;
+                st = trav_begin(sc, xyz(o), xyz(d), kInf);
+                has = sc.cnode_count != 0u;
+                if (!has) p.hit[id] = make_float2(kInf, 0.0f);
             } else {
-                warp_leaves_set_ray(wl, st);
+                id = item - n_ext;
+                const float4 o = p.shadow[3ull * id], d = p.shadow[3ull * id + 1];
+                const DevScene &sc = p.jobs[__float_as_uint(p.shadow[3ull * id + 2].w) >> 17].scene;
+                limit = o.w - 0.001f;
+                // Without cut-out materials the occlusion test may stop at the first triangle below
+                // the limit; with them the reference's closest-hit-then-alpha rule is kept.
+                any_hit = sc.any_hit_shadows != 0u;
+                st = trav_begin(sc, xyz(o), xyz(d), any_hit ? limit : kInf);
+                has = sc.cnode_count != 0u;
+                if (!has) {
+                    st.t = kInf;
+                    shadow_resolve(p, id, st, limit);
+                }
             }
+            if (has) warp_leaves_set_ray(wl, st);
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (uint32_t k = 0; k < steps; ++k) {
             if (trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
-                shadow_resolve(p, rec_i, st, limit);
+                if (occlusion) shadow_resolve(p, id, st, limit);
+                else p.hit[id] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
             }
             if (!__any_sync(0xFFFFFFFFu, has)) break;
@@ -776,13 +800,14 @@ bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
 
 namespace {
 
-using TravKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t);
+using ExtendKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t);
+using TraceKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t, uint32_t);
 
 template <int kStack, int kBlock>
-void pick(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
+void pick(const WaveTuning &t, ExtendKernel &ext, TraceKernel &trc) {
     if ((int)t.stack_entries == kStack && (int)t.block_threads == kBlock) {
         ext = wf_extend_kernel<kStack, kBlock>;
-        shd = wf_shadow_kernel<kStack, kBlock>;
+        trc = wf_trace_kernel<kStack, kBlock>;
     }
 }
 
@@ -791,8 +816,9 @@ size_t trav_smem_bytes(const WaveTuning &t) {
     return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves);
 }
 
-void trav_kernels(const WaveTuning &t, TravKernel &ext, TravKernel &shd) {
-    ext = shd = nullptr;
+void trav_kernels(const WaveTuning &t, ExtendKernel &ext, TraceKernel &shd) {
+    ext = nullptr;
+    shd = nullptr;
     pick<32, 64>(t, ext, shd);
     pick<32, 128>(t, ext, shd);
     pick<32, 256>(t, ext, shd);
@@ -811,17 +837,18 @@ void prepare_wavefront_kernels() {
     const int b64 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 64u});
     const int b48 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 48u});
     cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
-    cudaFuncSetAttribute(wf_shadow_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
+    cudaFuncSetAttribute(wf_trace_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
     cudaFuncSetAttribute(wf_extend_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
-    cudaFuncSetAttribute(wf_shadow_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
+    cudaFuncSetAttribute(wf_trace_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
 }
 
 cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
                           const WaveTuning &tune, cudaStream_t st) {
     WaveTuning t = tune;
     normalize_tuning(t, stack_need);
-    TravKernel ext, shd;
-    trav_kernels(t, ext, shd);
+    ExtendKernel ext;
+    TraceKernel trc;
+    trav_kernels(t, ext, trc);
     const size_t smem = trav_smem_bytes(t);
     const uint64_t blocks_needed = (max_items + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
@@ -844,19 +871,24 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     }
     WaveTuning t = tune;
     normalize_tuning(t, stack_need);
-    TravKernel ext, shd;
-    trav_kernels(t, ext, shd);
+    ExtendKernel ext;
+    TraceKernel trc;
+    trav_kernels(t, ext, trc);
     const size_t smem = trav_smem_bytes(t);
-    const uint64_t blocks_needed = (slots + t.block_threads - 1u) / t.block_threads;
+    // A launch carries up to one path per slot plus one occlusion ray per slot.
+    const uint64_t blocks_needed = (2u * slots + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);
     const uint64_t shade_needed = (slots + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
     const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
+    // extend(0), shade(0), then per iteration one trace launch with the occlusion rays of the
+    // iteration before and the closest-hit rays of this one, then its shade; the last occlusion rays
+    // close the pass.
     for (uint32_t it = 0; it < iters; ++it) {
-        ext<<<grid, t.block_threads, smem, st>>>(p, it, t.chunk, t.steps);
+        trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps);
         wf_shade_kernel<<<shade_grid, 128, 0, st>>>(p, it);
-        shd<<<grid, t.block_threads, smem, st>>>(p, it, t.chunk, t.steps);
     }
+    if (iters) trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
     for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);
     wf_count_kernel<<<1, 32, 0, st>>>(p, iters);
     return cudaGetLastError();

@@ -252,22 +252,14 @@ __device__ __forceinline__ float intersect_triangle(f3 ro, f3 rd, f3 v0, f3 v1, 
     return kInf;
 }
 
-struct Hit {
-    float t;
-    uint32_t prim;
-};
-
 // BVH traversal over the child-pair records.  Each record fetch tests both children's boxes with the
 // reference's slab test (gather.wgsl:71-75: (bmin - ro) / d, te <= ta && ta > 0 && te < t); leaf
 // children are intersected on the spot, internal children are visited nearest entry first with the
 // farther one pushed (a push is dropped once `stack_cap` entries are in use, as the reference drops
 // pushes at 63).  The tree is the reference's, so the closest hit is the reference's: only triangles
 // with exactly equal t may resolve to a different one of them.  The stack lives in shared memory, one
-// 4-byte column per thread.
-//
-// kAny: stop at the first triangle with t < t_limit (occlusion query); otherwise the closest hit below
-// t_limit.  TravState / trav_step make the traversal resumable one record at a time, so persistent
-// warps can refill lanes whose ray finished.
+// 4-byte column per thread.  TravState makes the traversal resumable one record at a time, so
+// persistent warps can refill lanes whose ray finished.
 struct TravState {
     f3 ro, rd, inv;
     float t;
@@ -291,92 +283,18 @@ __device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd,
     return st;
 }
 
-// Visits one record.  Returns true when the traversal has finished (st.t / st.prim hold the result;
-// for kAny, st.t < the limit means an occluder was found).
-template <bool kAny>
-__device__ __forceinline__ bool trav_step(TravState &st, uint32_t *stk, uint32_t stride) {
-    const float4 *np = st.cnodes + 4ull * st.node;
-    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-    const f3 ro = st.ro, rd = st.rd, inv = st.inv;
-    const f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
-    const f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
-    const float le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
-    const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
-    const float re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
-    const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
-    bool hl = le <= lx && lx > 0.0f && le < st.t;
-    bool hr = re <= rx && rx > 0.0f && re < st.t;
-    const uint32_t lref = __float_as_uint(q0.w), lcnt = __float_as_uint(q1.w);
-    const uint32_t rref = __float_as_uint(q2.w), rcnt = __float_as_uint(q3.w);
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-        const bool h = side == 0 ? hl : hr;
-        const uint32_t cnt = side == 0 ? lcnt : rcnt;
-        if (h && cnt) {
-            const uint32_t first = side == 0 ? lref : rref;
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const float4 *tp = st.tri_ord + 3ull * (first + k);
-                const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
-                // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
-                const f3 h3 = cross(rd, xyz(e2));
-                const float a = dot(xyz(e1), h3);
-                float t = kInf;
-                if (!(fabsf(a) < 1e-7f)) {
-                    const float f = 1.0f / a;
-                    const f3 sv = ro - xyz(v0);
-                    const float u = f * dot(sv, h3);
-                    if (!(u < 0.0f || u > 1.0f)) {
-                        const f3 q = cross(sv, xyz(e1));
-                        const float v = f * dot(rd, q);
-                        if (!(v < 0.0f || u + v > 1.0f)) {
-                            const float tt = f * dot(xyz(e2), q);
-                            if (tt > kEps) t = tt;
-                        }
-                    }
-                }
-                if (t < st.t) {
-                    st.t = t;
-                    st.prim = __float_as_uint(v0.w);
-                    if (kAny) return true;
-                }
-            }
-            if (side == 0) hl = false;
-            else hr = false;
-        }
-    }
-    if (hl && hr) {
-        const bool left_first = le <= re;
-        const uint32_t far = left_first ? rref : lref;
-        st.node = left_first ? lref : rref;
-        if (st.sp < st.cap) {
-            stk[st.sp * stride] = far;
-            st.sp += 1u;
-        }
-    } else if (hl) {
-        st.node = lref;
-    } else if (hr) {
-        st.node = rref;
-    } else {
-        if (st.sp == 0u) return true;
-        st.sp -= 1u;
-        st.node = stk[st.sp * stride];
-    }
-    return false;
-}
-
-// Warp-cooperative form of trav_step for the persistent traversal kernels.  Every lane of the warp
-// calls it together; `active` lanes advance their own traversal by one record exactly as trav_step
-// does, but the triangles of the record's hit leaves are tested by the whole warp: the leaf work of
-// all lanes is laid out as one list (lane order, left leaf before right leaf, triangles in leaf
-// order), cut into rounds of 32 tests, one per lane, and each lane then folds the results of its own
-// tests in list order with the reference's rule (a test wins when its t is strictly below the best so
-// far).  The result is trav_step's; only the lanes that do the arithmetic change.  With trav_step a
-// lane whose record holds four-triangle leaves tests them one after another while the rest of the
-// warp waits.
+// One traversal step for every lane of a warp; all 32 lanes call it together.  `active` lanes visit
+// their current record.  The triangles of the record's hit leaves are tested by the whole warp: the
+// leaf work of all lanes is laid out as one list (lane order, left leaf before right leaf, triangles
+// in leaf order), cut into rounds of 32 tests, one per lane, and each lane then folds the results of
+// its own tests in list order with the reference's rule (a test wins when its t is strictly below the
+// best so far), so a lane's result is what testing its leaves one by one gives.  Testing them one by
+// one in each lane instead leaves the warp waiting on the lanes with four-triangle leaves.
 //
-// `any` lanes stop at the first record whose leaves hold a triangle below st.t (the occlusion query);
-// st.t then holds the smallest such t of that record rather than the first.  WarpLeaves is per warp
-// and set_ray must have stored a lane's ray before its first step.
+// Returns true for an active lane whose traversal has finished (st.t / st.prim hold the closest hit
+// below the starting st.t).  `any` lanes (occlusion queries) also finish at the first record whose
+// leaves hold a triangle below st.t; st.t is then the smallest such t of that record.  WarpLeaves is
+// per warp, and warp_leaves_set_ray must have stored a lane's ray before its first step.
 struct WarpLeaves {
     float4 ray[2][32];  // per lane: (ro, low half of tri_ord), (rd, high half of tri_ord)
     uint32_t owner[32];
@@ -416,6 +334,32 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
     }
     const uint32_t nl = (hl && lcnt != 0u) ? lcnt : 0u;
     const uint32_t n = nl + ((hr && rcnt != 0u) ? rcnt : 0u);
+    // The next record does not depend on this record's leaf results (they only lower st.t for later
+    // box tests), so the lane moves on first and its next record is on the way to L1 while the warp
+    // tests leaves.
+    bool exhausted = false;
+    if (active) {
+        const bool il = hl && lcnt == 0u, ir = hr && rcnt == 0u;
+        if (il && ir) {
+            const bool left_first = le <= re;
+            const uint32_t far = left_first ? rref : lref;
+            st.node = left_first ? lref : rref;
+            if (st.sp < st.cap) {
+                stk[st.sp * stride] = far;
+                st.sp += 1u;
+            }
+        } else if (il) {
+            st.node = lref;
+        } else if (ir) {
+            st.node = rref;
+        } else if (st.sp == 0u) {
+            exhausted = true;
+        } else {
+            st.sp -= 1u;
+            st.node = stk[st.sp * stride];
+        }
+        if (!exhausted) asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 4ull * st.node));
+    }
     uint32_t incl = n;
 #pragma unroll
     for (uint32_t d = 1u; d < 32u; d <<= 1) {
@@ -451,7 +395,7 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
             const float4 *tp = tris + 3ull * tri;
             const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
             const f3 ro = xyz(r0), rd = xyz(r1);
-            // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed, as in trav_step.
+            // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
             const f3 h3 = cross(rd, xyz(e2));
             const float a = dot(xyz(e1), h3);
             if (!(fabsf(a) < 1e-7f)) {
@@ -484,41 +428,7 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
         }
         __syncwarp();
     }
-    if (!active) return false;
-    if (any && found) return true;
-    hl = hl && lcnt == 0u;
-    hr = hr && rcnt == 0u;
-    if (hl && hr) {
-        const bool left_first = le <= re;
-        const uint32_t far = left_first ? rref : lref;
-        st.node = left_first ? lref : rref;
-        if (st.sp < st.cap) {
-            stk[st.sp * stride] = far;
-            st.sp += 1u;
-        }
-    } else if (hl) {
-        st.node = lref;
-    } else if (hr) {
-        st.node = rref;
-    } else {
-        if (st.sp == 0u) return true;
-        st.sp -= 1u;
-        st.node = stk[st.sp * stride];
-    }
-    return false;
-}
-
-template <bool kAny>
-__device__ __forceinline__ Hit trace(const DevScene &s, f3 ro, f3 rd, float t_limit, uint32_t *stk,
-                                     uint32_t stride) {
-    if (s.cnode_count == 0u) return Hit{kInf, 0u};
-    TravState st = trav_begin(s, ro, rd, t_limit);
-    bool found = false;
-    while (!trav_step<kAny>(st, stk, stride)) {
-    }
-    if (kAny) found = st.t < t_limit;
-    if (kAny) return Hit{found ? st.t : kInf, st.prim};
-    return Hit{st.t, st.prim};
+    return active && (exhausted || (any && found));
 }
 
 struct Bary {
