@@ -318,8 +318,12 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
 }
 
 // ------------------------------------------------------------------------------------------------
-// shade: one bounce of gather.wgsl's loop body per queued path.
+// shade: one bounce of gather.wgsl's loop body per queued path.  kPhotons / kDebug compile the photon
+// lookup and the debug views in; the host picks the variant that covers every job of the launch
+// (a job without photons or debug view takes the same path through either variant), so frames
+// without them run a smaller kernel.
 // ------------------------------------------------------------------------------------------------
+template <bool kPhotons, bool kDebug>
 __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
@@ -417,7 +421,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                     add_radiance(sidx, A, thr * emis);
 
                     bool stop = false;
-                    if (debug_view != 0u) {  // gather.wgsl:359-419
+                    if (kDebug && debug_view != 0u) {  // gather.wgsl:359-419
                         const f3 half = mk3(0.5f, 0.5f, 0.5f);
                         stop = true;
                         switch (debug_view) {
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                             c_nee = thr * spec_ggx(wo, shn, ls.wi, a, f0) * ls.e / spec_prob;
                         }
                         bool nee_luma_only = false;
-                        if (ip.use_photons == 1u && !do_spec) {  // gather.wgsl:473-514
+                        if (kPhotons && ip.use_photons == 1u && !do_spec) {  // gather.wgsl:473-514
                             const rt_grid_params &gp = job.gp;
                             float r2 = ip.photon_radius * ip.photon_radius;
                             f3 ph_sum = mk3(0.0f, 0.0f, 0.0f);
@@ -583,7 +587,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                             rd = to_world(local, shn);
                             ro = hp + shn * 0.001f;
                             thr = thr * dscale;
-                            if (ip.use_photons == 1u) alive = false;
+                            if (kPhotons && ip.use_photons == 1u) alive = false;
                         }
                         if (alive) {
                             float pr = max3(thr);
@@ -884,9 +888,17 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     // extend(0), shade(0), then per iteration one trace launch with the occlusion rays of the
     // iteration before and the closest-hit rays of this one, then its shade; the last occlusion rays
     // close the pass.
+    bool photons = false, debug = false;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        photons = photons || jobs[j].photons != 0u;
+        debug = debug || jobs[j].debug != 0u;
+    }
+    void (*shade)(const WaveParams, uint32_t) =
+        photons ? (debug ? wf_shade_kernel<true, true> : wf_shade_kernel<true, false>)
+                : (debug ? wf_shade_kernel<false, true> : wf_shade_kernel<false, false>);
     for (uint32_t it = 0; it < iters; ++it) {
         trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps);
-        wf_shade_kernel<<<shade_grid, 128, 0, st>>>(p, it);
+        shade<<<shade_grid, 128, 0, st>>>(p, it);
     }
     if (iters) trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
     for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);

@@ -83,6 +83,8 @@ std::vector<unsigned char> BatchEngine::signature(rt_renderer *const *rs, uint32
         put(s, r->cfg.width);
         put(s, r->cfg.height);
         put(s, r->cfg.enable_denoise);
+        put(s, r->cfg.enable_photon_map);  // picks the shade kernel's variant
+        put(s, r->cfg.debug_view);
         put(s, r->cfg.denoise_passes);
         put(s, r->cfg.exposure);
         put(s, r->cfg.gamma);
@@ -100,7 +102,8 @@ int BatchEngine::enqueue(rt_renderer *const *rs, uint32_t n, uint32_t iters, con
     for (uint32_t j = 0; j < n; ++j) {
         const rt_renderer *r = rs[j];
         shapes[j] = rtd::JobShape{r->cfg.width, r->cfg.height, r->cfg.width * r->cfg.height, base[j],
-                                  r->scene.stack_cap};
+                                  r->scene.stack_cap, r->cfg.enable_photon_map ? 1u : 0u,
+                                  r->cfg.debug_view != 0u ? 1u : 0u};
     }
     const rtd::WaveParams wp = path.params(jobs.device(), n, counters.as<unsigned long long>());
     RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, tuning, stream));

@@ -45,6 +45,8 @@ struct WaveParams {
 // Host-side shape of a job for the per-job launches.
 struct JobShape {
     uint32_t width, height, npix, base, stack_cap;
+    uint32_t photons;  // the job gathers from a photon map (rt_image_params.use_photons)
+    uint32_t debug;    // the job renders a debug view (rt_image_params._pad[0] != 0)
 };
 // Launch shape of the persistent traversal kernels (extend, shadow); no effect on any result.
 struct WaveTuning {

@@ -529,7 +529,8 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     const rtd::DevJob job = rt::make_job(r, 0u);
     RT_CK(r->jobs.upload(&job, 1, s));
     const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
-    const rtd::JobShape shape{c.width, c.height, (uint32_t)npix, 0u, r->scene.stack_cap};
+    const rtd::JobShape shape{c.width,         c.height, (uint32_t)npix, 0u, r->scene.stack_cap,
+                              c.enable_photon_map ? 1u : 0u, c.debug_view != 0u ? 1u : 0u};
     RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
