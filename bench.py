@@ -386,10 +386,12 @@ def job_objects(spec: dict, pool):
 def frame_launches(cfgs) -> int:
     """Kernel launches of one batch frame over jobs with these configs: generate + finalize per job,
     per iteration one trace launch (closest-hit rays of the iteration with the occlusion rays of the
-    one before) and one shade, the closing trace launch, the counter kernel, then per job the denoise
-    passes and the resolve."""
+    one before), one shade and, when a job has a photon map, one photon-lookup launch; the closing
+    trace launch, the counter kernel, then per job the denoise passes and the resolve."""
     iters = max(max(c.spp, 1) * (c.max_bounces or 6) for c in cfgs)
-    return 2 * len(cfgs) + 2 * iters + 2 + sum((c.denoise_passes or 2) * int(c.enable_denoise) + 1 for c in cfgs)
+    per_iter = 3 if any(c.enable_photon_map for c in cfgs) else 2
+    return (2 * len(cfgs) + per_iter * iters + 2 +
+            sum((c.denoise_passes or 2) * int(c.enable_denoise) + 1 for c in cfgs))
 
 
 def batched_leg(n_jobs: int, steps: int, warmup: int, pool, seed: int = 4) -> dict:

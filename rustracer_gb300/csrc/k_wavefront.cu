@@ -35,18 +35,42 @@ struct Accum {
     float lum_sum, lum2_sum;
     float sl[8];
 };
+// The per-sample sums are selected with a compare per entry rather than an indexed store, so the
+// accumulator stays in registers.
+__device__ __forceinline__ void add_sample_luma(uint32_t s, Accum &a, float l) {
+#pragma unroll
+    for (uint32_t j = 0; j < 8u; ++j)
+        if (j == s) a.sl[j] += l;
+}
 __device__ __forceinline__ void add_radiance(uint32_t s, Accum &a, f3 c) {
     a.col = a.col + c;
     float l = luma(c);
     a.lum_sum += l;
     a.lum2_sum += l * l;
-    if (s < 8u) a.sl[s] += l;
+    add_sample_luma(s, a, l);
 }
 __device__ __forceinline__ void add_luma(uint32_t s, Accum &a, f3 c) {
     float l = luma(c);
     a.lum_sum += l;
     a.lum2_sum += l * l;
-    if (s < 8u) a.sl[s] += l;
+    add_sample_luma(s, a, l);
+}
+// add_radiance / add_luma of one term straight into a slot's accumulator in memory (the same
+// operations on the same values), touching only the words the term changes.
+__device__ __forceinline__ void acc_add_term(const WaveParams &p, uint32_t slot, uint32_t s, f3 c, bool luma_only) {
+    float4 *a = p.acc + 4 * (size_t)slot;
+    float4 a0 = a[0];
+    float *lum2 = reinterpret_cast<float *>(a + 1);
+    const float l = luma(c);
+    if (!luma_only) {
+        a0.x = a0.x + c.x;
+        a0.y = a0.y + c.y;
+        a0.z = a0.z + c.z;
+    }
+    a0.w += l;
+    a[0] = a0;
+    *lum2 += l * l;
+    if (s < 8u) reinterpret_cast<float *>(a + 2)[s] += l;
 }
 __device__ __forceinline__ Accum load_acc(const WaveParams &p, uint32_t pix) {
     const float4 a = p.acc[4 * (size_t)pix], b = p.acc[4 * (size_t)pix + 1], c = p.acc[4 * (size_t)pix + 2],
@@ -330,6 +354,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
     uint32_t *q_next = p.queue[(iter + 1u) & 1u];
     uint32_t *n_next = p.counts + 4 * (iter + 1u);
     uint32_t *n_shadow = p.counts + 4 * iter + 1u;
+    uint32_t *n_photon = p.counts + 4 * iter + 3u;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounds = (n + stride - 1u) / stride;
 
@@ -337,7 +362,9 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
         const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         const bool valid = i < n;
         bool keep = false;
-        bool emit_shadow = false;
+        bool emit_shadow = false, emit_photon = false;
+        f3 ph_hp = mk3(0.0f, 0.0f, 0.0f), ph_n = ph_hp, ph_td = ph_hp;
+        uint32_t ph_sidx = 0;
         uint32_t slot = 0;
         f3 sh_o = mk3(0.0f, 0.0f, 0.0f), sh_d = sh_o, sh_c = sh_o;
         float sh_max = 0.0f;
@@ -504,69 +531,16 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                         }
                         bool nee_luma_only = false;
                         if (kPhotons && ip.use_photons == 1u && !do_spec) {  // gather.wgsl:473-514
-                            const rt_grid_params &gp = job.gp;
-                            float r2 = ip.photon_radius * ip.photon_radius;
-                            f3 ph_sum = mk3(0.0f, 0.0f, 0.0f);
-                            uint32_t ph_hits = 0u, budget = 384u;
-                            bool done = false;
-                            int32_t bx = f2i_sat((hp.x - gp.room_min_x) / gp.cell_size);
-                            int32_t by = f2i_sat((hp.y - gp.room_min_y) / gp.cell_size);
-                            int32_t bz = f2i_sat((hp.z - gp.room_min_z) / gp.cell_size);
-                            int32_t gxmax = (int32_t)gp.grid_x - 1, gymax = (int32_t)gp.grid_y - 1,
-                                    gzmax = (int32_t)gp.grid_z - 1;
-                            for (int32_t dz = -1; dz <= 1 && !done; ++dz)
-                                for (int32_t dy = -1; dy <= 1 && !done; ++dy)
-                                    for (int32_t dx = -1; dx <= 1 && !done; ++dx) {
-                                        int32_t cx = clampi((int32_t)((uint32_t)bx + (uint32_t)dx), 0, gxmax);
-                                        int32_t cy = clampi((int32_t)((uint32_t)by + (uint32_t)dy), 0, gymax);
-                                        int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
-                                        uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x +
-                                                        (uint32_t)cz * gp.grid_x * gp.grid_y;
-                                        uint2 m = __ldg(job.grid_meta + cell);
-                                        // Photons in groups of four: the group's positions are loaded
-                                        // together (from the compact position array when there is
-                                        // one), then tested in order with the budget and hit cap.
-                                        for (uint32_t k = 0; k < m.y && !done; k += 4u) {
-                                            float4 pos[4];
-#pragma unroll
-                                            for (uint32_t j = 0; j < 4u; ++j) {
-                                                uint64_t idx = (uint64_t)m.x + k + j;
-                                                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                                                pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx)
-                                                                        : __ldg(job.sorted_photons + 4ull * idx);
-                                            }
-#pragma unroll
-                                            for (uint32_t j = 0; j < 4u; ++j) {
-                                                if (done || k + j >= m.y) break;
-                                                if (budget == 0u) {
-                                                    done = true;
-                                                    break;
-                                                }
-                                                budget -= 1u;
-                                                f3 dd = xyz(pos[j]) - hp;
-                                                float d2 = dot(dd, dd);
-                                                if (d2 < r2) {
-                                                    uint64_t idx = (uint64_t)m.x + k + j;
-                                                    idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                                                    const float4 *ph = job.sorted_photons + 4ull * idx;
-                                                    f3 pw = xyz(__ldg(ph + 1));
-                                                    f3 inc = xyz(__ldg(ph + 2));
-                                                    ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
-                                                    ph_hits += 1u;
-                                                    if (ph_hits >= 64u) done = true;
-                                                }
-                                            }
-                                        }
-                                    }
-                            if (ph_hits > 0u)
-                                add_radiance(sidx, A,
-                                             thr * dscale * ph_sum * ip.photon_scale /
-                                                 (kPi * (float)ph_hits * ip.photon_radius * ip.photon_radius));
-                            if (ip.photon_debug == 1u) {
-                                float density = fminf((float)ph_hits / 64.0f, 1.0f);
-                                A.col = mk3(1.0f - density, density, 0.0f) * 2.0f;
-                                nee_luma_only = true;  // the reference added the NEE term before this overwrite
-                            }
+                            // The lookup runs in wf_photon_kernel right after this pass; its term
+                            // lands before this bounce's NEE term, as here.  Photon debug mode
+                            // overwrites the colour after the lookup and keeps only the luminance of
+                            // the NEE term, whatever the lookup finds.
+                            emit_photon = true;
+                            ph_hp = hp;
+                            ph_n = shn;
+                            ph_td = thr * dscale;
+                            ph_sidx = sidx;
+                            if (ip.photon_debug == 1u) nee_luma_only = true;
                         }
                         if (ls.occlude && (c_nee.x != 0.0f || c_nee.y != 0.0f || c_nee.z != 0.0f)) {
                             emit_shadow = true;
@@ -633,7 +607,101 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                 }
             }
         }
+        if (kPhotons) {
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, emit_photon);
+            if (mask) {
+                const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(n_photon, (uint32_t)__popc(mask));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (emit_photon) {
+                    float4 *rec = p.preq + 3ull * (base + __popc(mask & lanemask_lt()));
+                    const uint32_t jid = __float_as_uint(p.thr[slot].w);
+                    rec[0] = make_float4(ph_hp.x, ph_hp.y, ph_hp.z, __uint_as_float(slot));
+                    rec[1] = make_float4(ph_n.x, ph_n.y, ph_n.z, __uint_as_float(ph_sidx));
+                    rec[2] = make_float4(ph_td.x, ph_td.y, ph_td.z, __uint_as_float(jid));
+                }
+            }
+        }
         warp_append(keep, slot, q_next, n_next);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// photon: the photon-map lookup of the diffuse bounces shade recorded (gather.wgsl:473-514), one
+// request per thread.  A separate pass keeps the shade kernel's registers (and its occupancy) off the
+// divergent cell loops.  Runs after shade(iter) and before the occlusion rays of iter, so a pixel's
+// terms arrive in the order the inline lookup added them.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) wf_photon_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+    const uint32_t n = p.counts[4 * iter + 3];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 r0 = p.preq[3ull * i], r1 = p.preq[3ull * i + 1], r2 = p.preq[3ull * i + 2];
+        const uint32_t slot = __float_as_uint(r0.w), sidx = __float_as_uint(r1.w);
+        const DevJob &job = p.jobs[__float_as_uint(r2.w)];
+        const rt_image_params &ip = job.ip;
+        const rt_grid_params &gp = job.gp;
+        const f3 hp = xyz(r0), shn = xyz(r1), td = xyz(r2);
+        const float r2max = ip.photon_radius * ip.photon_radius;
+        f3 ph_sum = mk3(0.0f, 0.0f, 0.0f);
+        uint32_t ph_hits = 0u, budget = 384u;
+        bool done = false;
+        const int32_t bx = f2i_sat((hp.x - gp.room_min_x) / gp.cell_size);
+        const int32_t by = f2i_sat((hp.y - gp.room_min_y) / gp.cell_size);
+        const int32_t bz = f2i_sat((hp.z - gp.room_min_z) / gp.cell_size);
+        const int32_t gxmax = (int32_t)gp.grid_x - 1, gymax = (int32_t)gp.grid_y - 1, gzmax = (int32_t)gp.grid_z - 1;
+        for (int32_t dz = -1; dz <= 1 && !done; ++dz)
+            for (int32_t dy = -1; dy <= 1 && !done; ++dy)
+                for (int32_t dx = -1; dx <= 1 && !done; ++dx) {
+                    const int32_t cx = clampi((int32_t)((uint32_t)bx + (uint32_t)dx), 0, gxmax);
+                    const int32_t cy = clampi((int32_t)((uint32_t)by + (uint32_t)dy), 0, gymax);
+                    const int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
+                    const uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x + (uint32_t)cz * gp.grid_x * gp.grid_y;
+                    const uint2 m = __ldg(job.grid_meta + cell);
+                    // Photons in groups of four: the group's positions are loaded together (from the
+                    // compact position array when there is one), then tested in order with the budget
+                    // and the hit cap.
+                    for (uint32_t k = 0; k < m.y && !done; k += 4u) {
+                        float4 pos[4];
+#pragma unroll
+                        for (uint32_t j = 0; j < 4u; ++j) {
+                            uint64_t idx = (uint64_t)m.x + k + j;
+                            idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                            pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx) : __ldg(job.sorted_photons + 4ull * idx);
+                        }
+#pragma unroll
+                        for (uint32_t j = 0; j < 4u; ++j) {
+                            if (done || k + j >= m.y) break;
+                            if (budget == 0u) {
+                                done = true;
+                                break;
+                            }
+                            budget -= 1u;
+                            const f3 dd = xyz(pos[j]) - hp;
+                            const float d2 = dot(dd, dd);
+                            if (d2 < r2max) {
+                                uint64_t idx = (uint64_t)m.x + k + j;
+                                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                                const float4 *ph = job.sorted_photons + 4ull * idx;
+                                const f3 pw = xyz(__ldg(ph + 1));
+                                const f3 inc = xyz(__ldg(ph + 2));
+                                ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
+                                ph_hits += 1u;
+                                if (ph_hits >= 64u) done = true;
+                            }
+                        }
+                    }
+                }
+        if (ph_hits > 0u)
+            acc_add_term(p, slot, sidx,
+                         td * ph_sum * ip.photon_scale / (kPi * (float)ph_hits * ip.photon_radius * ip.photon_radius),
+                         false);
+        if (ip.photon_debug == 1u) {
+            const float density = fminf((float)ph_hits / 64.0f, 1.0f);
+            const f3 col = mk3(1.0f - density, density, 0.0f) * 2.0f;
+            float4 *a = p.acc + 4 * (size_t)slot;
+            a[0] = make_float4(col.x, col.y, col.z, a[0].w);
+        }
     }
 }
 
@@ -654,12 +722,7 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
         }
     }
     if (shadowed) return;
-    const uint32_t slot = __float_as_uint(d.w);
-    Accum A = load_acc(p, slot);
-    const float4 acc1 = p.acc[4 * (size_t)slot + 1];
-    if (tag & 0x10000u) add_luma(tag & 0xFFFFu, A, xyz(c));
-    else add_radiance(tag & 0xFFFFu, A, xyz(c));
-    store_acc(p, slot, A, acc1);
+    acc_add_term(p, __float_as_uint(d.w), tag & 0xFFFFu, xyz(c), (tag & 0x10000u) != 0u);
 }
 
 // trace: the occlusion rays of iteration `shd_iter` and the closest-hit rays of iteration `ext_iter` in
@@ -670,7 +733,7 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
 constexpr uint32_t kNoIter = 0xFFFFFFFFu;
 
 template <int kStack, int kBlock>
-__global__ void __launch_bounds__(kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
+__global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
                                                           uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
@@ -678,7 +741,9 @@ __global__ void __launch_bounds__(kBlock) wf_trace_kernel(const __grid_constant_
     const uint32_t n_ext = ext_iter != kNoIter ? p.counts[4 * ext_iter] : 0u;
     const uint32_t n_shd = shd_iter != kNoIter ? p.counts[4 * shd_iter + 1] : 0u;
     const uint32_t *q = p.queue[ext_iter & 1u];
-    uint32_t *fetch = ext_iter != kNoIter ? p.counts + 4 * ext_iter + 2 : p.counts + 4 * shd_iter + 3;
+    // Row ext_iter's cursor; the closing launch (no closest-hit rays) takes row shd_iter + 1's, which
+    // no other launch uses.  Entry [3] of a row counts shade's photon-lookup requests.
+    uint32_t *fetch = p.counts + 4 * (ext_iter != kNoIter ? ext_iter : shd_iter + 1u) + 2;
     WarpFeed feed;
     TravState st;
     bool has = false, occlusion = false, any_hit = false;
@@ -885,6 +950,8 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);
     const uint64_t shade_needed = (slots + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
     const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
+    const uint64_t photon_cap = (uint64_t)num_sms * 16u;
+    const uint32_t photon_grid = (uint32_t)(shade_needed < photon_cap ? shade_needed : photon_cap);
     // extend(0), shade(0), then per iteration one trace launch with the occlusion rays of the
     // iteration before and the closest-hit rays of this one, then its shade; the last occlusion rays
     // close the pass.
@@ -899,6 +966,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     for (uint32_t it = 0; it < iters; ++it) {
         trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps);
         shade<<<shade_grid, 128, 0, st>>>(p, it);
+        if (photons) wf_photon_kernel<<<photon_grid, 128, 0, st>>>(p, it);
     }
     if (iters) trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
     for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);

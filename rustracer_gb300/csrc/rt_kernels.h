@@ -38,8 +38,9 @@ struct WaveParams {
     float4 *acc;       // 4 per slot: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
     float4 *nrm;       // first-hit shading normal
     uint32_t *queue[2];
-    uint32_t *counts;  // per iteration: [0] paths queued, [1] shadow rays, [2] / [3] fetch cursors
+    uint32_t *counts;  // per iteration: [0] paths queued, [1] shadow rays, [2] trace cursor, [3] photon lookups
     float4 *shadow;    // 3 per deferred NEE ray: (origin, max_dist), (dir, slot), (contribution, tag)
+    float4 *preq;      // 3 per photon-map lookup: (hit point, slot), (normal, sample), (throughput, job)
     unsigned long long *counters;  // [0] segments, [1] shadow rays (cumulative)
 };
 // Host-side shape of a job for the per-job launches.

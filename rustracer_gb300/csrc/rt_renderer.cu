@@ -6,7 +6,8 @@
 //           as rgba8 arrays (layer-major); the traversal layout derived from the reference's BVH:
 //           one 64 B record per internal node, one 48 B leaf-ordered triangle record per prim slot.
 //   path:   per pixel, origin / direction / throughput (16 B each), hit 8 B, accumulators 64 B,
-//           first normal 16 B, two queue entries 4 B, one deferred shadow ray 48 B (192 B / pixel).
+//           first normal 16 B, two queue entries 4 B, one deferred shadow ray 48 B, one photon-lookup
+//           request 48 B (240 B / pixel).
 //   frame:  frame, denoise ping-pong, moments, gbuffer, accumulation (float4 per pixel each) and the
 //           rgba8 output image.
 //   photon: photon slots (64 B, 6 per photon), u32 key per slot, slot order, sorted photons (64 B),
@@ -253,9 +254,9 @@ uint64_t rt_renderer::device_bytes() const {
                  d_sorted_pos.bytes + d_rank.bytes +
                  d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
                  d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
-    const rt::DevBuf *pb[10] = {&path.ro, &path.rd, &path.thr, &path.hit, &path.acc,
-                                &path.nrm, &path.queue[0], &path.queue[1], &path.shadow, &path.counts};
-    for (int i = 0; i < 9; ++i) n += pb[i]->bytes;
+    const rt::DevBuf *pb[10] = {&path.ro,       &path.rd,       &path.thr,    &path.hit,  &path.acc,
+                                &path.nrm,      &path.queue[0], &path.queue[1], &path.shadow, &path.preq};
+    for (int i = 0; i < 10; ++i) n += pb[i]->bytes;
     return n;
 }
 
@@ -339,7 +340,7 @@ void resident_scene_release(rt_resident_scene *s) {
 }
 
 uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
-    return slots * 192u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
+    return slots * 240u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
 }
 
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {

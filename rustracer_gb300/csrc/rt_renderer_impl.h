@@ -87,17 +87,17 @@ struct FrameEventRing {
     }
 };
 
-// Wavefront path state for `slots` pixel slots (192 B per slot) and the per-iteration counters.
+// Wavefront path state for `slots` pixel slots (240 B per slot) and the per-iteration counters.
 struct PathState {
-    DevBuf ro, rd, thr, hit, acc, nrm, queue[2], shadow, counts;
+    DevBuf ro, rd, thr, hit, acc, nrm, queue[2], shadow, preq, counts;
     size_t slots = 0, counts_bytes = 0;
     // (Re)allocates when too small.  The caller's stream must be idle.
     cudaError_t ensure(size_t n_slots, uint32_t iters) {
         cudaError_t e;
         if (n_slots > slots) {
-            DevBuf *b[9] = {&ro, &rd, &thr, &nrm, &hit, &acc, &queue[0], &queue[1], &shadow};
-            const size_t sz[9] = {16, 16, 16, 16, 8, 64, 4, 4, 48};
-            for (int i = 0; i < 9; ++i)
+            DevBuf *b[10] = {&ro, &rd, &thr, &nrm, &hit, &acc, &queue[0], &queue[1], &shadow, &preq};
+            const size_t sz[10] = {16, 16, 16, 16, 8, 64, 4, 4, 48, 48};
+            for (int i = 0; i < 10; ++i)
                 if ((e = b[i]->alloc(n_slots * sz[i])) != cudaSuccess) {
                     slots = 0;
                     return e;
@@ -129,6 +129,7 @@ struct PathState {
         w.queue[1] = queue[1].as<uint32_t>();
         w.counts = counts.as<uint32_t>();
         w.shadow = shadow.as<float4>();
+        w.preq = preq.as<float4>();
         w.counters = counters;
         return w;
     }
