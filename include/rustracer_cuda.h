@@ -583,6 +583,15 @@ int rt_bvh_build_gpu(const float *centroids, const float *bbox_min, const float 
 /* Threads of the host BVH build (0, the default: one per hardware thread; 1: sequential).  The
  * tree does not depend on it. */
 void rt_set_host_threads(uint32_t n);
+/* Children per traversal record for scenes uploaded from now on (rt_renderer_create,
+ * rt_resident_scene_create, the server's scene uploads): 4 (the default) adds a four-wide copy of
+ * the scene's tree -- each record takes in the children of its largest internal children -- walked
+ * whenever every job of a launch has one (a scene whose four-wide walk could need more than 64 stack
+ * entries keeps only the two-wide records); 2 keeps the two-wide records only.  Either walk finds the
+ * reference's closest hit; only triangles hit at exactly equal t may resolve to a different one of
+ * them.  Returns RT_ERR_INVALID_ARGUMENT for other widths. */
+int rt_set_traversal_width(uint32_t width);
+uint32_t rt_get_traversal_width(void);
 
 /* PNG scanline unfiltering for the glTF ingest (the reference decodes images through the `gltf` /
  * `image` crates, rustracer-core/src/loader.rs:36-100): h rows of 1 + stride bytes (filter type

@@ -299,7 +299,7 @@ cudaError_t launch_photon_wave(const PhotonTraceParams &p, const PhotonWave &w, 
     const uint64_t shade_needed = (n + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
     const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
     for (uint32_t it = 0; it < RT_MAX_BOUNCES; ++it) {
-        if ((e = launch_extend(wp, it, n, p.scene.stack_cap, num_sms, tune, st)) != cudaSuccess) return e;
+        if ((e = launch_extend(wp, it, n, p.scene, num_sms, tune, st)) != cudaSuccess) return e;
         ph_shade_kernel<<<shade_grid, 128, 0, st>>>(p, w, it);
     }
     return cudaGetLastError();

@@ -302,7 +302,7 @@ __device__ __forceinline__ uint32_t warp_take(WarpFeed &f, bool need, uint32_t n
 }
 
 // extend: closest hit of each queued path (any job: each lane traces its own job's scene).
-template <int kStack, int kBlock>
+template <int kStack, int kBlock, bool kWide>
 __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant__ WaveParams p, uint32_t iter,
                                                            uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
             slot = q[item];
             const float4 o = p.ro[slot], d = p.rd[slot];
             const DevScene &sc = p.jobs[__float_as_uint(p.thr[slot].w)].scene;
-            st = trav_begin(sc, xyz(o), xyz(d), kInf);
+            st = trav_begin<kWide>(sc, xyz(o), xyz(d), kInf, (uint32_t)kStack);
             has = true;
             if (sc.cnode_count == 0u) {
                 p.hit[slot] = make_float2(kInf, 0.0f);
@@ -332,7 +332,8 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (uint32_t k = 0; k < steps; ++k) {
-            if (trav_step_warp(st, has, false, stk, (uint32_t)kBlock, wl)) {
+            if (kWide ? trav_step_warp4(st, has, false, stk, (uint32_t)kBlock, wl)
+                      : trav_step_warp(st, has, false, stk, (uint32_t)kBlock, wl)) {
                 p.hit[slot] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
             }
@@ -732,7 +733,7 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
 // start early and the shorter occlusion rays fill the end.
 constexpr uint32_t kNoIter = 0xFFFFFFFFu;
 
-template <int kStack, int kBlock>
+template <int kStack, int kBlock, bool kWide>
 __global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
                                                           uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __
                 const float4 o = p.ro[id], d = p.rd[id];
                 const DevScene &sc = p.jobs[__float_as_uint(p.thr[id].w)].scene;
                 any_hit = false;
-                st = trav_begin(sc, xyz(o), xyz(d), kInf);
+                st = trav_begin<kWide>(sc, xyz(o), xyz(d), kInf, (uint32_t)kStack);
                 has = sc.cnode_count != 0u;
                 if (!has) p.hit[id] = make_float2(kInf, 0.0f);
             } else {
@@ -769,7 +770,7 @@ __global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __
                 // Without cut-out materials the occlusion test may stop at the first triangle below
                 // the limit; with them the reference's closest-hit-then-alpha rule is kept.
                 any_hit = sc.any_hit_shadows != 0u;
-                st = trav_begin(sc, xyz(o), xyz(d), any_hit ? limit : kInf);
+                st = trav_begin<kWide>(sc, xyz(o), xyz(d), any_hit ? limit : kInf, (uint32_t)kStack);
                 has = sc.cnode_count != 0u;
                 if (!has) {
                     st.t = kInf;
@@ -780,7 +781,8 @@ __global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (uint32_t k = 0; k < steps; ++k) {
-            if (trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
+            if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl)
+                      : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
                 else p.hit[id] = make_float2(st.t, __uint_as_float(st.prim));
                 has = false;
@@ -873,10 +875,10 @@ using ExtendKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t);
 using TraceKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t, uint32_t);
 
 template <int kStack, int kBlock>
-void pick(const WaveTuning &t, ExtendKernel &ext, TraceKernel &trc) {
+void pick(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &trc) {
     if ((int)t.stack_entries == kStack && (int)t.block_threads == kBlock) {
-        ext = wf_extend_kernel<kStack, kBlock>;
-        trc = wf_trace_kernel<kStack, kBlock>;
+        ext = wide ? wf_extend_kernel<kStack, kBlock, true> : wf_extend_kernel<kStack, kBlock, false>;
+        trc = wide ? wf_trace_kernel<kStack, kBlock, true> : wf_trace_kernel<kStack, kBlock, false>;
     }
 }
 
@@ -885,39 +887,56 @@ size_t trav_smem_bytes(const WaveTuning &t) {
     return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves);
 }
 
-void trav_kernels(const WaveTuning &t, ExtendKernel &ext, TraceKernel &shd) {
+void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &shd) {
     ext = nullptr;
     shd = nullptr;
-    pick<32, 64>(t, ext, shd);
-    pick<32, 128>(t, ext, shd);
-    pick<32, 256>(t, ext, shd);
-    pick<48, 64>(t, ext, shd);
-    pick<48, 128>(t, ext, shd);
-    pick<48, 256>(t, ext, shd);
-    pick<64, 64>(t, ext, shd);
-    pick<64, 128>(t, ext, shd);
-    pick<64, 256>(t, ext, shd);
+    pick<32, 64>(t, wide, ext, shd);
+    pick<32, 128>(t, wide, ext, shd);
+    pick<32, 256>(t, wide, ext, shd);
+    pick<48, 64>(t, wide, ext, shd);
+    pick<48, 128>(t, wide, ext, shd);
+    pick<48, 256>(t, wide, ext, shd);
+    pick<64, 64>(t, wide, ext, shd);
+    pick<64, 128>(t, wide, ext, shd);
+    pick<64, 256>(t, wide, ext, shd);
 }
 
 }  // namespace
 
-void prepare_wavefront_kernels() {
-    // Blocks above 48 KB of dynamic shared memory (64- and 48-entry stacks x 256 lanes) need the opt-in.
-    const int b64 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 64u});
-    const int b48 = (int)trav_smem_bytes(WaveTuning{256u, 1u, 64u, 8u, 48u});
-    cudaFuncSetAttribute(wf_extend_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
-    cudaFuncSetAttribute(wf_trace_kernel<64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b64);
-    cudaFuncSetAttribute(wf_extend_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
-    cudaFuncSetAttribute(wf_trace_kernel<48, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, b48);
+template <int kStack, int kBlock, bool kWide>
+void opt_in_smem() {
+    // Blocks above 48 KB of dynamic shared memory need the opt-in; set it for every shape.
+    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack});
+    cudaFuncSetAttribute(wf_extend_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
+template <bool kWide>
+void opt_in_all() {
+    opt_in_smem<32, 64, kWide>();
+    opt_in_smem<32, 128, kWide>();
+    opt_in_smem<32, 256, kWide>();
+    opt_in_smem<48, 64, kWide>();
+    opt_in_smem<48, 128, kWide>();
+    opt_in_smem<48, 256, kWide>();
+    opt_in_smem<64, 64, kWide>();
+    opt_in_smem<64, 128, kWide>();
+    opt_in_smem<64, 256, kWide>();
+}
+
+void prepare_wavefront_kernels() {
+    opt_in_all<false>();
+    opt_in_all<true>();
+}
+
+cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, const DevScene &scene, int num_sms,
                           const WaveTuning &tune, cudaStream_t st) {
+    const bool wide = scene.wnodes != nullptr;
     WaveTuning t = tune;
-    normalize_tuning(t, stack_need);
+    normalize_tuning(t, wide ? scene.wide_stack : scene.stack_cap);
     ExtendKernel ext;
     TraceKernel trc;
-    trav_kernels(t, ext, trc);
+    trav_kernels(t, wide, ext, trc);
     const size_t smem = trav_smem_bytes(t);
     const uint64_t blocks_needed = (max_items + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
@@ -931,18 +950,21 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     cudaError_t e;
     if ((e = cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4 * (size_t)(iters + 1), st)) != cudaSuccess) return e;
     uint64_t slots = 0;
-    uint32_t stack_need = 0;
+    uint32_t stack_need = 0, wide_need = 0;
+    bool wide = n_jobs > 0;  // four-wide records when every job's scene has them
     for (uint32_t j = 0; j < n_jobs; ++j) {
         const uint32_t tiles = ((jobs[j].width + 7u) / 8u) * ((jobs[j].height + 3u) / 4u);
         wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p, j);
         slots += jobs[j].npix;
         stack_need = jobs[j].stack_cap > stack_need ? jobs[j].stack_cap : stack_need;
+        wide_need = jobs[j].wide_stack > wide_need ? jobs[j].wide_stack : wide_need;
+        wide = wide && jobs[j].wide != 0u;
     }
     WaveTuning t = tune;
-    normalize_tuning(t, stack_need);
+    normalize_tuning(t, wide ? wide_need : stack_need);
     ExtendKernel ext;
     TraceKernel trc;
-    trav_kernels(t, ext, trc);
+    trav_kernels(t, wide, ext, trc);
     const size_t smem = trav_smem_bytes(t);
     // A launch carries up to one path per slot plus one occlusion ray per slot.
     const uint64_t blocks_needed = (2u * slots + t.block_threads - 1u) / t.block_threads;

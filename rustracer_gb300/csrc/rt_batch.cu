@@ -89,6 +89,8 @@ std::vector<unsigned char> BatchEngine::signature(rt_renderer *const *rs, uint32
         put(s, r->cfg.exposure);
         put(s, r->cfg.gamma);
         put(s, r->scene.stack_cap);
+        put(s, r->scene.wnodes);  // picks the traversal kernels
+        put(s, r->scene.wide_stack);
         put(s, r->glow);
         put(s, r->marker);
         put(s, base[j]);
@@ -103,7 +105,8 @@ int BatchEngine::enqueue(rt_renderer *const *rs, uint32_t n, uint32_t iters, con
         const rt_renderer *r = rs[j];
         shapes[j] = rtd::JobShape{r->cfg.width, r->cfg.height, r->cfg.width * r->cfg.height, base[j],
                                   r->scene.stack_cap, r->cfg.enable_photon_map ? 1u : 0u,
-                                  r->cfg.debug_view != 0u ? 1u : 0u};
+                                  r->cfg.debug_view != 0u ? 1u : 0u, r->scene.wnodes ? 1u : 0u,
+                                  r->scene.wide_stack};
     }
     const rtd::WaveParams wp = path.params(jobs.device(), n, counters.as<unsigned long long>());
     RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, tuning, stream));
@@ -244,8 +247,15 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
     const GraphMode saved_mode = graph_mode;
     graph_mode = GraphMode::Off;
 
-    uint32_t stack_need = 0;
-    for (uint32_t j = 0; j < n; ++j) stack_need = std::max(stack_need, rs[j]->scene.stack_cap);
+    // The stack the launches will need (four-wide records when every job's scene has them).
+    uint32_t stack_two = 0, stack_four = 0;
+    bool wide = n > 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        stack_two = std::max(stack_two, rs[j]->scene.stack_cap);
+        stack_four = std::max(stack_four, rs[j]->scene.wide_stack);
+        wide = wide && rs[j]->scene.wnodes != nullptr;
+    }
+    const uint32_t stack_need = wide ? stack_four : stack_two;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     RT_CK(cudaEventCreate(&e0));
     RT_CK(cudaEventCreate(&e1));

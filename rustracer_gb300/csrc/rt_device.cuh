@@ -125,6 +125,11 @@ struct DevScene {
     const float4 *cnodes;
     const float4 *tri_ord;
     uint32_t cnode_count, stack_cap;
+    // The same tree with up to four children per 128-byte record (per child (min, ref), (max, count);
+    // count 0xFFFFFFFF marks an empty place), when a near-first walk of it needs at most 64 stack
+    // entries (wide_stack); otherwise wnodes is null and only the two-wide records are used.
+    const float4 *wnodes;
+    uint32_t wnode_count, wide_stack;
     uint32_t any_hit_shadows;  // 1: no alpha-cutout material, shadow rays may stop at the first hit
     const float4 *tris;      // 8 x float4 per TriangleGpu
     const float4 *mats;      // 4 x float4 per MaterialGpu
@@ -268,11 +273,16 @@ struct TravState {
     uint32_t cap;                    // stack entries this scene may use
 };
 
-__device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd, float t_limit) {
+// kWide: walk the four-wide records with the lane's whole stack (stack_entries, at least
+// s.wide_stack, so no push is dropped); otherwise the two-wide records with the reference's push
+// limit (s.stack_cap, at most stack_entries).
+template <bool kWide>
+__device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd, float t_limit,
+                                                uint32_t stack_entries) {
     TravState st;
-    st.cnodes = s.cnodes;
+    st.cnodes = kWide ? s.wnodes : s.cnodes;
     st.tri_ord = s.tri_ord;
-    st.cap = s.stack_cap;
+    st.cap = kWide ? stack_entries : s.stack_cap;
     st.ro = ro;
     st.rd = rd;
     st.inv = mk3(1.0f, 1.0f, 1.0f) / rd;
@@ -297,6 +307,8 @@ __device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd,
 // per warp, and warp_leaves_set_ray must have stored a lane's ray before its first step.
 struct WarpLeaves {
     float4 ray[2][32];  // per lane: (ro, low half of tri_ord), (rd, high half of tri_ord)
+    uint4 leaf_ref[32];    // four-wide step: per lane the first prim slot of each hit leaf
+    uint4 leaf_start[32];  // and where its tests start in the lane's run (0xFFFFFFFF: none)
     uint32_t owner[32];
     float t[32];
     uint32_t prim[32];
@@ -307,6 +319,82 @@ __device__ __forceinline__ void warp_leaves_set_ray(WarpLeaves &w, const TravSta
     const unsigned long long tp = (unsigned long long)st.tri_ord;
     w.ray[0][lane] = make_float4(st.ro.x, st.ro.y, st.ro.z, __uint_as_float((uint32_t)tp));
     w.ray[1][lane] = make_float4(st.rd.x, st.rd.y, st.rd.z, __uint_as_float((uint32_t)(tp >> 32)));
+}
+
+// The leaf tests of one traversal step for the whole warp: lane l has n_l tests (its run), laid out
+// in lane order and cut into rounds of 32; tri_of(owner, j) gives the prim slot of the owner's j-th
+// test (every lane calls it, with its own arguments).  Each lane folds its own results in run order
+// into st.t / st.prim (a test wins when its t is strictly below the best so far) and returns whether
+// any of them won.
+template <typename TriOf>
+__device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, WarpLeaves &w, TriOf tri_of) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+#pragma unroll
+    for (uint32_t d = 1u; d < 32u; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t excl = incl - n;
+    bool found = false;
+    for (uint32_t base = 0u; base < total; base += 32u) {
+        // This round tests list entries [base, base + 32); a lane owning some of them marks where its
+        // run starts, so every position finds its owner as the last start at or below it.
+        const uint32_t lo = excl > base ? excl : base;
+        const uint32_t hi = excl + n < base + 32u ? excl + n : base + 32u;
+        const bool mine = lo < hi;
+        if (mine) w.owner[lo - base] = lane;
+        const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, mine ? 1u << (lo - base) : 0u);
+        __syncwarp();
+        const uint32_t start = 31u - __clz((starts | 1u) & (0xFFFFFFFFu >> (31u - lane)));
+        const uint32_t o = w.owner[start];
+        const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, excl, o);
+        const uint32_t o_tri = tri_of(o, base + lane - o_excl);  // every lane calls: shuffles inside
+        float t = kInf;
+        uint32_t prim = 0u;
+        if (base + lane < total) {
+            const float4 r0 = w.ray[0][o], r1 = w.ray[1][o];
+            const float4 *tris = reinterpret_cast<const float4 *>(
+                ((unsigned long long)__float_as_uint(r1.w) << 32) | (unsigned long long)__float_as_uint(r0.w));
+            const uint32_t tri = o_tri;
+            const float4 *tp = tris + 3ull * tri;
+            const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+            const f3 ro = xyz(r0), rd = xyz(r1);
+            // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
+            const f3 h3 = cross(rd, xyz(e2));
+            const float a = dot(xyz(e1), h3);
+            if (!(fabsf(a) < 1e-7f)) {
+                const float f = 1.0f / a;
+                const f3 sv = ro - xyz(v0);
+                const float u = f * dot(sv, h3);
+                if (!(u < 0.0f || u > 1.0f)) {
+                    const f3 q = cross(sv, xyz(e1));
+                    const float v = f * dot(rd, q);
+                    if (!(v < 0.0f || u + v > 1.0f)) {
+                        const float tt = f * dot(xyz(e2), q);
+                        if (tt > kEps) t = tt;
+                    }
+                }
+            }
+            prim = __float_as_uint(v0.w);
+        }
+        w.t[lane] = t;
+        w.prim[lane] = prim;
+        __syncwarp();
+        if (mine) {
+            for (uint32_t k = lo - base; k < hi - base; ++k) {
+                const float tk = w.t[k];
+                if (tk < st.t) {
+                    st.t = tk;
+                    st.prim = w.prim[k];
+                    found = true;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    return found;
 }
 
 __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
@@ -360,74 +448,101 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
         }
         if (!exhausted) asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 4ull * st.node));
     }
-    uint32_t incl = n;
-#pragma unroll
-    for (uint32_t d = 1u; d < 32u; d <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (lane >= d) incl += v;
-    }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    const uint32_t excl = incl - n;
-    bool found = false;
-    for (uint32_t base = 0u; base < total; base += 32u) {
-        // This round tests list entries [base, base + 32); a lane owning some of them marks where its
-        // run starts, so every position finds its owner as the last start at or below it.
-        const uint32_t lo = excl > base ? excl : base;
-        const uint32_t hi = excl + n < base + 32u ? excl + n : base + 32u;
-        const bool mine = lo < hi;
-        if (mine) w.owner[lo - base] = lane;
-        const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, mine ? 1u << (lo - base) : 0u);
-        __syncwarp();
-        const uint32_t start = 31u - __clz((starts | 1u) & (0xFFFFFFFFu >> (31u - lane)));
-        const uint32_t o = w.owner[start];
-        const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, excl, o);
+    const bool found = warp_leaf_rounds(st, n, w, [&](uint32_t o, uint32_t j) {
         const uint32_t o_nl = __shfl_sync(0xFFFFFFFFu, nl, o);
         const uint32_t o_lref = __shfl_sync(0xFFFFFFFFu, lref, o);
         const uint32_t o_rref = __shfl_sync(0xFFFFFFFFu, rref, o);
-        float t = kInf;
-        uint32_t prim = 0u;
-        if (base + lane < total) {
-            const float4 r0 = w.ray[0][o], r1 = w.ray[1][o];
-            const float4 *tris = reinterpret_cast<const float4 *>(
-                ((unsigned long long)__float_as_uint(r1.w) << 32) | (unsigned long long)__float_as_uint(r0.w));
-            const uint32_t j = base + lane - o_excl;
-            const uint32_t tri = j < o_nl ? o_lref + j : o_rref + (j - o_nl);
-            const float4 *tp = tris + 3ull * tri;
-            const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
-            const f3 ro = xyz(r0), rd = xyz(r1);
-            // Moller-Trumbore (common.wgsl:78-100) with the edges precomputed.
-            const f3 h3 = cross(rd, xyz(e2));
-            const float a = dot(xyz(e1), h3);
-            if (!(fabsf(a) < 1e-7f)) {
-                const float f = 1.0f / a;
-                const f3 sv = ro - xyz(v0);
-                const float u = f * dot(sv, h3);
-                if (!(u < 0.0f || u > 1.0f)) {
-                    const f3 q = cross(sv, xyz(e1));
-                    const float v = f * dot(rd, q);
-                    if (!(v < 0.0f || u + v > 1.0f)) {
-                        const float tt = f * dot(xyz(e2), q);
-                        if (tt > kEps) t = tt;
+        return j < o_nl ? o_lref + j : o_rref + (j - o_nl);
+    });
+    return active && (exhausted || (any && found));
+}
+
+// trav_step_warp over the four-wide records: each active lane tests the four child boxes of its
+// record with the same slab test, queues the hit leaves' triangles (child order) for the warp's leaf
+// rounds, and visits the hit internal children nearest entry first (the others pushed, farthest
+// first; the stack holds every pending entry).  Same results as the two-wide walk: the closest hit
+// below the starting st.t, only triangles with exactly equal t may resolve to another of them.
+__device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
+                                                WarpLeaves &w) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t n = 0u;
+    bool exhausted = false;
+    if (active) {
+        const float4 *np = st.cnodes + 8ull * st.node;
+        float4 q[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) q[i] = __ldg(np + i);
+        const f3 ro = st.ro, inv = st.inv;
+        float key[4];
+        uint32_t ref[4];
+        uint32_t lr[4] = {0u, 0u, 0u, 0u}, ls[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+        uint32_t n_leaf = 0u;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const f3 a0 = (xyz(q[2 * c]) - ro) * inv, a1 = (xyz(q[2 * c + 1]) - ro) * inv;
+            const float te = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
+            const float tx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
+            const uint32_t cref = __float_as_uint(q[2 * c].w), cnt = __float_as_uint(q[2 * c + 1].w);
+            const bool hit = cnt != 0xFFFFFFFFu && te <= tx && tx > 0.0f && te < st.t;
+            ref[c] = cref;
+            key[c] = (hit && cnt == 0u) ? te : __int_as_float(0x7F800000);  // +inf: not a pending child
+            if (hit && cnt != 0u) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if ((uint32_t)i == n_leaf) {
+                        lr[i] = cref;
+                        ls[i] = n;
                     }
-                }
-            }
-            prim = __float_as_uint(v0.w);
-        }
-        w.t[lane] = t;
-        w.prim[lane] = prim;
-        __syncwarp();
-        if (mine) {
-            for (uint32_t k = lo - base; k < hi - base; ++k) {
-                const float tk = w.t[k];
-                if (tk < st.t) {
-                    st.t = tk;
-                    st.prim = w.prim[k];
-                    found = true;
-                }
+                n_leaf += 1u;
+                n += cnt;
             }
         }
-        __syncwarp();
+        if (n != 0u) {
+            w.leaf_ref[lane] = make_uint4(lr[0], lr[1], lr[2], lr[3]);
+            w.leaf_start[lane] = make_uint4(ls[0], ls[1], ls[2], ls[3]);
+        }
+        // Near-first order of the hit internal children (a fixed five-exchange network).
+        auto cswap = [&](int i, int j) {
+            if (key[j] < key[i]) {
+                const float tk = key[i];
+                key[i] = key[j];
+                key[j] = tk;
+                const uint32_t tr = ref[i];
+                ref[i] = ref[j];
+                ref[j] = tr;
+            }
+        };
+        cswap(0, 1);
+        cswap(2, 3);
+        cswap(0, 2);
+        cswap(1, 3);
+        cswap(1, 2);
+        const float kNone = __int_as_float(0x7F800000);
+        const uint32_t m = (key[0] < kNone ? 1u : 0u) + (key[1] < kNone ? 1u : 0u) + (key[2] < kNone ? 1u : 0u) +
+                           (key[3] < kNone ? 1u : 0u);
+        if (m != 0u) {
+            st.node = ref[0];
+#pragma unroll
+            for (int i = 3; i >= 1; --i)
+                if ((uint32_t)i < m && st.sp < st.cap) {
+                    stk[st.sp * stride] = ref[i];
+                    st.sp += 1u;
+                }
+        } else if (st.sp == 0u) {
+            exhausted = true;
+        } else {
+            st.sp -= 1u;
+            st.node = stk[st.sp * stride];
+        }
+        if (!exhausted) asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 8ull * st.node));
     }
+    const bool found = warp_leaf_rounds(st, n, w, [&](uint32_t o, uint32_t j) {
+        const uint4 r = w.leaf_ref[o], b = w.leaf_start[o];
+        const uint32_t i = (j >= b.y ? 1u : 0u) + (j >= b.z ? 1u : 0u) + (j >= b.w ? 1u : 0u);
+        const uint32_t first = i == 0u ? r.x : (i == 1u ? r.y : (i == 2u ? r.z : r.w));
+        const uint32_t at = i == 0u ? b.x : (i == 1u ? b.y : (i == 2u ? b.z : b.w));
+        return first + (j - at);
+    });
     return active && (exhausted || (any && found));
 }
 

@@ -11,6 +11,7 @@
 // Compiled with -ffp-contract=off so results are identical on x86-64 and AArch64 hosts; values that
 // need a transcendental function are computed in double precision and rounded once.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -354,6 +355,104 @@ bool build_traversal_layout(const rt_bvh_node *nodes, uint64_t n_nodes, const ui
     }
     (void)f2bits;
     return true;
+}
+
+void build_wide_layout(const rt_bvh_node *nodes, uint64_t n_nodes, WideLayout &out) {
+    out.nodes.clear();
+    out.stack_need = 0;
+    if (n_nodes == 0) return;
+    auto area = [&](uint32_t i) {
+        const rt_bvh_node &n = nodes[i];
+        const float dx = n.bbox_max[0] - n.bbox_min[0], dy = n.bbox_max[1] - n.bbox_min[1],
+                    dz = n.bbox_max[2] - n.bbox_min[2];
+        return dx * dy + dy * dz + dz * dx;
+    };
+    // Records in breadth-first order: rec_src[r] is the binary node whose subtree record r covers.
+    std::vector<uint32_t> rec_src;
+    std::vector<std::array<uint32_t, 4>> kids;  // binary node of each place (0xFFFFFFFF: empty)
+    rec_src.push_back(0);
+    for (size_t r = 0; r < rec_src.size(); ++r) {
+        std::array<uint32_t, 4> k;
+        k.fill(0xFFFFFFFFu);
+        uint32_t cnt = 0;
+        const rt_bvh_node &root = nodes[rec_src[r]];
+        if (root.prim_count > 0) {  // a tree that is one leaf: one record holding that leaf
+            k[cnt++] = rec_src[r];
+        } else {
+            k[cnt++] = root.left_first;
+            k[cnt++] = root.right_child;
+            while (cnt < 4u) {
+                int best = -1;
+                float best_a = -1.0f;
+                for (uint32_t i = 0; i < cnt; ++i)
+                    if (nodes[k[i]].prim_count == 0 && area(k[i]) > best_a) {
+                        best = (int)i;
+                        best_a = area(k[i]);
+                    }
+                if (best < 0) break;
+                const rt_bvh_node &n = nodes[k[best]];
+                for (uint32_t i = cnt; i > (uint32_t)best + 1u; --i) k[i] = k[i - 1];
+                k[best] = n.left_first;
+                k[best + 1] = n.right_child;
+                ++cnt;
+            }
+        }
+        kids.push_back(k);
+        for (uint32_t i = 0; i < cnt; ++i)
+            if (nodes[k[i]].prim_count == 0) rec_src.push_back(k[i]);
+    }
+    const size_t n_rec = rec_src.size();
+    out.nodes.assign(n_rec * 32, 0.0f);
+    std::vector<uint32_t> need(n_rec, 0);
+    // Children get their record numbers in the order the breadth-first pass queued them.
+    std::vector<uint32_t> first_child(n_rec, 0);
+    uint32_t next = 1;
+    for (size_t r = 0; r < n_rec; ++r) {
+        first_child[r] = next;
+        for (uint32_t i = 0; i < 4; ++i)
+            if (kids[r][i] != 0xFFFFFFFFu && nodes[kids[r][i]].prim_count == 0) ++next;
+    }
+    for (size_t r = 0; r < n_rec; ++r) {
+        float *q = &out.nodes[r * 32];
+        uint32_t child_rec = first_child[r];
+        for (uint32_t i = 0; i < 4; ++i) {
+            float *c = q + 8 * i;
+            const uint32_t b = kids[r][i];
+            if (b == 0xFFFFFFFFu) {
+                c[3] = bits2f(0u);
+                c[7] = bits2f(0xFFFFFFFFu);
+                continue;
+            }
+            const rt_bvh_node &n = nodes[b];
+            for (int a = 0; a < 3; ++a) {
+                c[a] = n.bbox_min[a];
+                c[4 + a] = n.bbox_max[a];
+            }
+            if (n.prim_count > 0) {
+                c[3] = bits2f(n.left_first);
+                c[7] = bits2f(n.prim_count);
+            } else {
+                c[3] = bits2f(child_rec++);
+                c[7] = bits2f(0u);
+            }
+        }
+    }
+    // Stack bound, children before parents (breadth-first numbers grow downwards).
+    for (size_t r = n_rec; r-- > 0;) {
+        uint32_t internal = 0, deepest = 0;
+        const float *q = &out.nodes[r * 32];
+        for (uint32_t i = 0; i < 4; ++i) {
+            uint32_t cnt, ref;
+            std::memcpy(&cnt, q + 8 * i + 7, 4);
+            std::memcpy(&ref, q + 8 * i + 3, 4);
+            if (cnt == 0u) {
+                ++internal;
+                deepest = std::max(deepest, need[ref]);
+            }
+        }
+        need[r] = internal ? internal - 1u + deepest : 0u;
+    }
+    out.stack_need = need[0];
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1148,6 +1247,22 @@ extern "C" int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride,
 }
 
 extern "C" void rt_set_host_threads(uint32_t n) { g_host_threads.store(n); }
+
+namespace {
+std::atomic<uint32_t> g_traversal_width{4u};
+}
+uint32_t rt::traversal_width() { return g_traversal_width.load(); }
+
+extern "C" int rt_set_traversal_width(uint32_t width) {
+    rt::clear_error();
+    if (width != 2u && width != 4u) {
+        rt::set_error("rt_set_traversal_width: width must be 2 or 4, got %u", width);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    g_traversal_width.store(width);
+    return RT_OK;
+}
+extern "C" uint32_t rt_get_traversal_width(void) { return g_traversal_width.load(); }
 
 extern "C" int rt_scene_set_bvh_builder(rt_scene *s, uint32_t builder) {
     if (!s || builder > RT_BVH_GPU_LBVH) {

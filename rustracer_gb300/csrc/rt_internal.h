@@ -65,6 +65,20 @@ struct TraversalLayout {
 bool build_traversal_layout(const rt_bvh_node *nodes, uint64_t n_nodes, const uint32_t *prims, uint64_t n_prims,
                             const rt_triangle *tris, uint64_t n_tris, TraversalLayout &out);
 
+// The same tree with every record holding up to four children: each record of the two-wide layout
+// absorbs the children of its largest (surface area) internal child until it has four (leaves stay
+// the reference's leaves, with the same prim slots).  32 floats per record: per child (min, ref) and
+// (max, count), count > 0 a leaf of `count` prim slots from `ref`, count 0 an internal child whose
+// record is `ref`, count 0xFFFFFFFF an empty place.  `stack_need` bounds the entries a near-first
+// walk holds at once (the internal children of a record minus one, summed along a root-to-leaf path).
+struct WideLayout {
+    std::vector<float> nodes;  // 32 per record
+    uint32_t stack_need = 0;
+};
+void build_wide_layout(const rt_bvh_node *nodes, uint64_t n_nodes, WideLayout &out);
+// rt_set_traversal_width: 4 (the default) or 2; read when a scene is uploaded.
+uint32_t traversal_width();
+
 }  // namespace rt
 
 struct rt_scene {

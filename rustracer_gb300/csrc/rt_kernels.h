@@ -48,6 +48,8 @@ struct JobShape {
     uint32_t width, height, npix, base, stack_cap;
     uint32_t photons;  // the job gathers from a photon map (rt_image_params.use_photons)
     uint32_t debug;    // the job renders a debug view (rt_image_params._pad[0] != 0)
+    uint32_t wide;     // the job's scene has four-wide records (DevScene.wnodes)
+    uint32_t wide_stack;  // stack entries a walk of them can need
 };
 // Launch shape of the persistent traversal kernels (extend, shadow); no effect on any result.
 struct WaveTuning {
@@ -95,7 +97,7 @@ cudaError_t launch_photon_wave(const PhotonTraceParams &p, const PhotonWave &w, 
                                const WaveTuning &tune, cudaStream_t st);
 // One closest-hit pass of the persistent traversal kernel over queue[iter & 1] (count at
 // counts[4 iter]); `max_items` bounds the grid.
-cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, uint32_t stack_need, int num_sms,
+cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items, const DevScene &scene, int num_sms,
                           const WaveTuning &tune, cudaStream_t st);
 
 // Photon grid (exact u32 counting sort).  Scratch sizes come from grid_scratch_bytes.

@@ -294,6 +294,15 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
                                     sd->triangles, sd->triangle_count, lay))
         return fail(RT_ERR_INVALID_ARGUMENT);
     if ((st = upload(res->d_cnodes, lay.cnodes.data(), lay.cnodes.size(), s)) != RT_OK) return fail(st);
+    // The four-wide records when the library traverses four-wide and a walk of them fits the largest
+    // shared-memory stack without dropping a push.
+    rt::WideLayout wide;
+    if (rt::traversal_width() == 4u && sd->bvh_node_count > 0) {
+        rt::build_wide_layout(sd->bvh_nodes, sd->bvh_node_count, wide);
+        if (wide.stack_need > 64u) wide.nodes.clear();
+        if (!wide.nodes.empty() && (st = upload(res->d_wnodes, wide.nodes.data(), wide.nodes.size(), s)) != RT_OK)
+            return fail(st);
+    }
     if ((st = upload(res->d_tri_ord, lay.tri_ord.data(), lay.tri_ord.size(), s)) != RT_OK) return fail(st);
     if ((st = upload(res->d_mats, sd->materials, sd->material_count, s)) != RT_OK) return fail(st);
     res->lights.assign(sd->lights, sd->lights + sd->light_count);
@@ -301,6 +310,9 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
     ds.cnodes = res->d_cnodes.as<float4>();
     ds.tri_ord = res->d_tri_ord.as<float4>();
     ds.cnode_count = (uint32_t)(lay.cnodes.size() / 16);
+    ds.wnodes = wide.nodes.empty() ? nullptr : res->d_wnodes.as<float4>();
+    ds.wnode_count = (uint32_t)(wide.nodes.size() / 32);
+    ds.wide_stack = wide.nodes.empty() ? 0u : wide.stack_need;
     // A near-first traversal holds at most one pending entry per tree level.
     ds.stack_cap = lay.max_depth < 32u ? 32u : 63u;
     ds.any_hit_shadows = 1u;
@@ -329,7 +341,7 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
         res->bmax[i] = sd->bounds_max[i];
     }
     res->has_bounds = sd->has_bounds;
-    res->bytes = res->d_cnodes.bytes + res->d_tri_ord.bytes + res->d_tris.bytes + res->d_mats.bytes +
+    res->bytes = res->d_cnodes.bytes + res->d_wnodes.bytes + res->d_tri_ord.bytes + res->d_tris.bytes + res->d_mats.bytes +
                  res->d_tex[0].bytes + res->d_tex[1].bytes + res->d_tex[2].bytes + res->d_tex[3].bytes;
     *out = res;
     return RT_OK;
@@ -530,8 +542,15 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     const rtd::DevJob job = rt::make_job(r, 0u);
     RT_CK(r->jobs.upload(&job, 1, s));
     const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
-    const rtd::JobShape shape{c.width,         c.height, (uint32_t)npix, 0u, r->scene.stack_cap,
-                              c.enable_photon_map ? 1u : 0u, c.debug_view != 0u ? 1u : 0u};
+    const rtd::JobShape shape{c.width,
+                              c.height,
+                              (uint32_t)npix,
+                              0u,
+                              r->scene.stack_cap,
+                              c.enable_photon_map ? 1u : 0u,
+                              c.debug_view != 0u ? 1u : 0u,
+                              r->scene.wnodes ? 1u : 0u,
+                              r->scene.wide_stack};
     RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));

@@ -181,7 +181,7 @@ struct JobTable {
 struct rt_resident_scene {
     int device = 0;
     std::atomic<uint32_t> refs{1};
-    rt::DevBuf d_cnodes, d_tri_ord, d_tris, d_mats, d_tex[4];
+    rt::DevBuf d_cnodes, d_wnodes, d_tri_ord, d_tris, d_mats, d_tex[4];
     rtd::DevScene scene{};          // light fields are per renderer
     std::vector<rt_light> lights;   // the scene's lights, each renderer's initial copy
     float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};

@@ -67,7 +67,8 @@ struct Flight {
 };
 
 uint64_t scene_estimate(const rt_scene_desc &d) {
-    uint64_t b = d.triangle_count * 128 + d.bvh_node_count * 64 + d.bvh_prim_count * 48 + d.material_count * 64 + 64;
+    // two-wide records (at most one per node) and four-wide records (at most 128 B per two nodes)
+    uint64_t b = d.triangle_count * 128 + d.bvh_node_count * 128 + d.bvh_prim_count * 48 + d.material_count * 64 + 64;
     const rt_texture_array *t[4] = {&d.tex_albedo, &d.tex_mr, &d.tex_emissive, &d.tex_normal};
     for (auto *x : t)
         if (x->rgba8) b += (uint64_t)x->width * x->height * x->layers * 4;

@@ -379,6 +379,17 @@ class Batch:
         return t.as_dict(), float(ms.value)
 
 
+def set_traversal_width(width: int) -> None:
+    """Children per traversal record for scenes uploaded from now on: 4 (default) or 2
+    (rt_set_traversal_width)."""
+    lib = A.load()
+    A.check("rt_set_traversal_width", lib.rt_set_traversal_width(int(width)))
+
+
+def traversal_width() -> int:
+    return int(A.load().rt_get_traversal_width())
+
+
 def render_config_default() -> RenderConfig:
     """RenderConfig::default() as the native library defines it."""
     c = A.RenderConfigC()

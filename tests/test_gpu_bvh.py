@@ -79,3 +79,43 @@ def test_gpu_and_host_trees_render_the_same_image(gpu):
         assert scene.bvh_builder_used() == builder
     # the same closest hits except where two triangles lie at exactly the same distance
     assert match_frac(imgs[1], imgs[0]) >= FRAC
+
+
+@pytest.fixture
+def width2():
+    """Scenes uploaded inside the test keep only the two-wide records."""
+    rt.set_traversal_width(2)
+    yield
+    rt.set_traversal_width(4)
+
+
+def test_two_wide_walk_matches_the_oracle(gpu, orc, width2):
+    scene = rt.Scene.icosphere_room(level=4, seed=3, sigma=0.02, tex_size=32)
+    cfg = rt.RenderConfig(width=64, height=48, spp=2, accumulate_frames=3, enable_denoise=False)
+    r, o = render_both(orc, scene, cfg, 3)
+    assert match_frac(r.read_accumulation(), o.accum) >= FRAC
+
+
+def test_four_and_two_wide_walks_render_the_same_image(gpu):
+    imgs, sizes = [], []
+    for width in (4, 2):
+        rt.set_traversal_width(width)
+        try:
+            scene = rt.Scene.icosphere_room(level=5, seed=6, sigma=0.02, tex_size=32)
+            res = rt.ResidentScene(scene)
+            sizes.append(res.device_bytes())
+            cfg = rt.RenderConfig(width=80, height=60, spp=2, accumulate_frames=2, enable_denoise=False,
+                                  enable_photon_map=True, photon_count=4096)
+            r = rt.Renderer(res, cfg)
+            r.update_camera(scene.default_camera())
+            r.rebuild_photons()
+            r.render_frames(2)
+            imgs.append(r.read_accumulation())
+            r.close()
+            res.close()
+        finally:
+            rt.set_traversal_width(4)
+    assert sizes[0] > sizes[1]  # the four-wide records ride along with the two-wide ones
+    # the same closest hits except where two triangles lie at exactly the same distance
+    assert match_frac(imgs[0], imgs[1]) >= FRAC
+

@@ -83,3 +83,13 @@ def test_backend_struct_sizes_match_the_header():
     assert A.Request.config.offset == 16 and A.Request.camera.offset == 112
     assert C.sizeof(A.JobStatus) == 48
     assert C.sizeof(A.ServerStats) == 128
+
+
+def test_traversal_width_setting():
+    """rt_set_traversal_width takes 2 or 4 and nothing else (no device needed)."""
+    lib = A.load()
+    assert lib.rt_get_traversal_width() == 4
+    assert lib.rt_set_traversal_width(8) == A.RT_ERR_INVALID_ARGUMENT
+    assert b"width must be 2 or 4" in lib.rt_last_error()
+    assert lib.rt_set_traversal_width(2) == 0 and lib.rt_get_traversal_width() == 2
+    assert lib.rt_set_traversal_width(4) == 0 and lib.rt_get_traversal_width() == 4
