@@ -35,28 +35,22 @@ struct Accum {
     float lum_sum, lum2_sum;
     float sl[8];
 };
-// The per-sample sums are selected with a compare per entry rather than an indexed store, so the
-// accumulator stays in registers.
-__device__ __forceinline__ void add_sample_luma(uint32_t s, Accum &a, float l) {
-#pragma unroll
-    for (uint32_t j = 0; j < 8u; ++j)
-        if (j == s) a.sl[j] += l;
-}
-__device__ __forceinline__ void add_radiance(uint32_t s, Accum &a, f3 c) {
+// The words of a slot's accumulator one shade step can change: every term it adds belongs to the
+// sample it started with, so only that sample's luminance sum is loaded and stored with the colour
+// and the two luminance moments.
+struct PathAcc {
+    f3 col;
+    float lum_sum, lum2_sum, sl;
+};
+__device__ __forceinline__ void add_radiance(uint32_t s, PathAcc &a, f3 c) {
     a.col = a.col + c;
     float l = luma(c);
     a.lum_sum += l;
     a.lum2_sum += l * l;
-    add_sample_luma(s, a, l);
+    if (s < 8u) a.sl += l;
 }
-__device__ __forceinline__ void add_luma(uint32_t s, Accum &a, f3 c) {
-    float l = luma(c);
-    a.lum_sum += l;
-    a.lum2_sum += l * l;
-    add_sample_luma(s, a, l);
-}
-// add_radiance / add_luma of one term straight into a slot's accumulator in memory (the same
-// operations on the same values), touching only the words the term changes.
+// One radiance term (or only its luminance) added straight into a slot's accumulator in memory:
+// colour, the two luminance moments and the sample's luminance sum, as every path step adds them.
 __device__ __forceinline__ void acc_add_term(const WaveParams &p, uint32_t slot, uint32_t s, f3 c, bool luma_only) {
     float4 *a = p.acc + 4 * (size_t)slot;
     float4 a0 = a[0];
@@ -82,12 +76,6 @@ __device__ __forceinline__ Accum load_acc(const WaveParams &p, uint32_t pix) {
     A.sl[0] = c.x; A.sl[1] = c.y; A.sl[2] = c.z; A.sl[3] = c.w;
     A.sl[4] = d.x; A.sl[5] = d.y; A.sl[6] = d.z; A.sl[7] = d.w;
     return A;
-}
-__device__ __forceinline__ void store_acc(const WaveParams &p, uint32_t pix, const Accum &A, float4 b_rest) {
-    p.acc[4 * (size_t)pix] = make_float4(A.col.x, A.col.y, A.col.z, A.lum_sum);
-    p.acc[4 * (size_t)pix + 1] = make_float4(A.lum2_sum, b_rest.y, b_rest.z, b_rest.w);
-    p.acc[4 * (size_t)pix + 2] = make_float4(A.sl[0], A.sl[1], A.sl[2], A.sl[3]);
-    p.acc[4 * (size_t)pix + 3] = make_float4(A.sl[4], A.sl[5], A.sl[6], A.sl[7]);
 }
 
 __device__ __forceinline__ f3 sky_color(f3 dir, f3 zenith, f3 horizon, float intensity) {
@@ -392,9 +380,13 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
             uint32_t sidx = sb & 0xFFFFu, b = sb >> 16;
             const float hit_t = h2.x;
             const uint32_t prim = __float_as_uint(h2.y);
-            Accum A = load_acc(p, slot);
-            float4 acc1 = p.acc[4 * (size_t)slot + 1];  // .y = first_depth
-            float4 nrm = p.nrm[slot];
+            float4 *acc = p.acc + 4 * (size_t)slot;
+            const uint32_t sidx0 = sidx;
+            const float4 acc0 = acc[0];
+            float4 acc1 = acc[1];  // .x = lum2_sum, .y = first_depth
+            PathAcc A{xyz(acc0), acc0.w, acc1.x, sidx0 < 8u ? reinterpret_cast<const float *>(acc + 2)[sidx0] : 0.0f};
+            bool first_hit = false;  // this step found a nearer first hit (normal and depth change)
+            float4 nrm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             bool alive = true;  // the sample continues with another segment
 
             if (hit_t >= kInf) {
@@ -428,6 +420,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                     }
                     if (b == 0u && hit_t < acc1.y) {
                         nrm = make_float4(sn.x, sn.y, sn.z, 0.0f);
+                        first_hit = true;
                         acc1.y = hit_t;
                     }
                     f3 albedo = mat.albedo;
@@ -589,8 +582,10 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
             p.ro[slot] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(rng.state));
             p.rd[slot] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(pack_sb(sidx, b)));
             p.thr[slot] = make_float4(thr.x, thr.y, thr.z, __uint_as_float(jid));
-            store_acc(p, slot, A, acc1);
-            p.nrm[slot] = nrm;
+            acc[0] = make_float4(A.col.x, A.col.y, A.col.z, A.lum_sum);
+            acc[1] = make_float4(A.lum2_sum, acc1.y, acc1.z, acc1.w);
+            if (sidx0 < 8u) reinterpret_cast<float *>(acc + 2)[sidx0] = A.sl;
+            if (first_hit) p.nrm[slot] = nrm;
         }
         // NEE shadow ray (deferred) and the continuing path.
         {

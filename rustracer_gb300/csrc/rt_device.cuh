@@ -399,7 +399,6 @@ __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, Warp
 
 __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
                                                WarpLeaves &w) {
-    const uint32_t lane = threadIdx.x & 31u;
     bool hl = false, hr = false;
     float le = 0.0f, re = 0.0f;
     uint32_t lref = 0u, lcnt = 0u, rref = 0u, rcnt = 0u;
