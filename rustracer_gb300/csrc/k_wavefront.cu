@@ -729,7 +729,7 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
 constexpr uint32_t kNoIter = 0xFFFFFFFFu;
 
 template <int kStack, int kBlock, bool kWide>
-__global__ void __launch_bounds__(kBlock, 896 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
+__global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
                                                           uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
