@@ -646,48 +646,57 @@ __global__ void __launch_bounds__(128) wf_photon_kernel(const __grid_constant__ 
         const int32_t by = f2i_sat((hp.y - gp.room_min_y) / gp.cell_size);
         const int32_t bz = f2i_sat((hp.z - gp.room_min_z) / gp.cell_size);
         const int32_t gxmax = (int32_t)gp.grid_x - 1, gymax = (int32_t)gp.grid_y - 1, gzmax = (int32_t)gp.grid_z - 1;
-        for (int32_t dz = -1; dz <= 1 && !done; ++dz)
-            for (int32_t dy = -1; dy <= 1 && !done; ++dy)
-                for (int32_t dx = -1; dx <= 1 && !done; ++dx) {
-                    const int32_t cx = clampi((int32_t)((uint32_t)bx + (uint32_t)dx), 0, gxmax);
-                    const int32_t cy = clampi((int32_t)((uint32_t)by + (uint32_t)dy), 0, gymax);
-                    const int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
-                    const uint32_t cell = (uint32_t)cx + (uint32_t)cy * gp.grid_x + (uint32_t)cz * gp.grid_x * gp.grid_y;
-                    const uint2 m = __ldg(job.grid_meta + cell);
-                    // Photons in groups of four: the group's positions are loaded together (from the
-                    // compact position array when there is one), then tested in order with the budget
-                    // and the hit cap.
-                    for (uint32_t k = 0; k < m.y && !done; k += 4u) {
-                        float4 pos[4];
+        // The 27 cells in the reference's order (dz, then dy, then dx), walked as one flat loop over
+        // (cell, photon group) so each thread moves to its next cell on its own instead of the warp
+        // waiting at every cell for its fullest one.
+        auto cell_at = [&](uint32_t i) {
+            const int32_t dz = (int32_t)(i / 9u) - 1, dy = (int32_t)((i / 3u) % 3u) - 1, dx = (int32_t)(i % 3u) - 1;
+            const int32_t cx = clampi((int32_t)((uint32_t)bx + (uint32_t)dx), 0, gxmax);
+            const int32_t cy = clampi((int32_t)((uint32_t)by + (uint32_t)dy), 0, gymax);
+            const int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
+            return (uint32_t)cx + (uint32_t)cy * gp.grid_x + (uint32_t)cz * gp.grid_x * gp.grid_y;
+        };
+        uint32_t ci = 0u, k = 0u;
+        uint2 m = __ldg(job.grid_meta + cell_at(0u));
+        while (!done) {
+            if (k >= m.y) {
+                if (++ci >= 27u) break;
+                m = __ldg(job.grid_meta + cell_at(ci));
+                k = 0u;
+                continue;
+            }
+            // A group of four photons: positions loaded together (from the compact position array
+            // when there is one), then tested in order with the budget and the hit cap.
+            float4 pos[4];
 #pragma unroll
-                        for (uint32_t j = 0; j < 4u; ++j) {
-                            uint64_t idx = (uint64_t)m.x + k + j;
-                            idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                            pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx) : __ldg(job.sorted_photons + 4ull * idx);
-                        }
+            for (uint32_t j = 0; j < 4u; ++j) {
+                uint64_t idx = (uint64_t)m.x + k + j;
+                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx) : __ldg(job.sorted_photons + 4ull * idx);
+            }
 #pragma unroll
-                        for (uint32_t j = 0; j < 4u; ++j) {
-                            if (done || k + j >= m.y) break;
-                            if (budget == 0u) {
-                                done = true;
-                                break;
-                            }
-                            budget -= 1u;
-                            const f3 dd = xyz(pos[j]) - hp;
-                            const float d2 = dot(dd, dd);
-                            if (d2 < r2max) {
-                                uint64_t idx = (uint64_t)m.x + k + j;
-                                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                                const float4 *ph = job.sorted_photons + 4ull * idx;
-                                const f3 pw = xyz(__ldg(ph + 1));
-                                const f3 inc = xyz(__ldg(ph + 2));
-                                ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
-                                ph_hits += 1u;
-                                if (ph_hits >= 64u) done = true;
-                            }
-                        }
-                    }
+            for (uint32_t j = 0; j < 4u; ++j) {
+                if (done || k + j >= m.y) break;
+                if (budget == 0u) {
+                    done = true;
+                    break;
                 }
+                budget -= 1u;
+                const f3 dd = xyz(pos[j]) - hp;
+                const float d2 = dot(dd, dd);
+                if (d2 < r2max) {
+                    uint64_t idx = (uint64_t)m.x + k + j;
+                    idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
+                    const float4 *ph = job.sorted_photons + 4ull * idx;
+                    const f3 pw = xyz(__ldg(ph + 1));
+                    const f3 inc = xyz(__ldg(ph + 2));
+                    ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
+                    ph_hits += 1u;
+                    if (ph_hits >= 64u) done = true;
+                }
+            }
+            k += 4u;
+        }
         if (ph_hits > 0u)
             acc_add_term(p, slot, sidx,
                          td * ph_sum * ip.photon_scale / (kPi * (float)ph_hits * ip.photon_radius * ip.photon_radius),
