@@ -656,11 +656,17 @@ __global__ void __launch_bounds__(128) wf_photon_kernel(const __grid_constant__ 
             const int32_t cz = clampi((int32_t)((uint32_t)bz + (uint32_t)dz), 0, gzmax);
             return (uint32_t)cx + (uint32_t)cy * gp.grid_x + (uint32_t)cz * gp.grid_x * gp.grid_y;
         };
+        // Photon indices are u32 and clamped to the last sorted photon (the backend's rule for an
+        // out-of-range index; the grid's ranges never leave the array).
+        const uint32_t last = (uint32_t)job.sorted_count - 1u;
+        const float4 *posv = job.sorted_pos ? job.sorted_pos : job.sorted_photons;
+        const uint32_t pstride = job.sorted_pos ? 1u : 4u;
         uint32_t ci = 0u, k = 0u;
         uint2 m = __ldg(job.grid_meta + cell_at(0u));
+        if (job.sorted_count == 0u) m.y = 0u, ci = 27u;
         while (!done) {
             if (k >= m.y) {
-                if (++ci >= 27u) break;
+                if (++ci >= 27u) break;  // also ends at once for an empty photon map
                 m = __ldg(job.grid_meta + cell_at(ci));
                 k = 0u;
                 continue;
@@ -669,11 +675,7 @@ __global__ void __launch_bounds__(128) wf_photon_kernel(const __grid_constant__ 
             // when there is one), then tested in order with the budget and the hit cap.
             float4 pos[4];
 #pragma unroll
-            for (uint32_t j = 0; j < 4u; ++j) {
-                uint64_t idx = (uint64_t)m.x + k + j;
-                idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                pos[j] = job.sorted_pos ? __ldg(job.sorted_pos + idx) : __ldg(job.sorted_photons + 4ull * idx);
-            }
+            for (uint32_t j = 0; j < 4u; ++j) pos[j] = __ldg(posv + (size_t)min(m.x + k + j, last) * pstride);
 #pragma unroll
             for (uint32_t j = 0; j < 4u; ++j) {
                 if (done || k + j >= m.y) break;
@@ -685,9 +687,7 @@ __global__ void __launch_bounds__(128) wf_photon_kernel(const __grid_constant__ 
                 const f3 dd = xyz(pos[j]) - hp;
                 const float d2 = dot(dd, dd);
                 if (d2 < r2max) {
-                    uint64_t idx = (uint64_t)m.x + k + j;
-                    idx = idx < job.sorted_count ? idx : job.sorted_count - 1;
-                    const float4 *ph = job.sorted_photons + 4ull * idx;
+                    const float4 *ph = job.sorted_photons + 4ull * min(m.x + k + j, last);
                     const f3 pw = xyz(__ldg(ph + 1));
                     const f3 inc = xyz(__ldg(ph + 2));
                     ph_sum = ph_sum + pw * fmaxf(dot(shn, -inc), 0.0f);
