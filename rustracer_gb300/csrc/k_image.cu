@@ -95,6 +95,11 @@ __device__ __forceinline__ float ex2_approx(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 template <int kStep, bool kInterior, bool kPow12>
 __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * kStep],
@@ -132,18 +137,17 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
                     if (ny < 0 || ny >= Hh || y0 + k * kStep >= Hh) continue;
                 }
                 const float d = fmaxf(cn[k].x * nd.x + cn[k].y * nd.y + cn[k].z * nd.z, 0.0f);
-                float nw;
-                if (kPow12) {
-                    const float d2 = d * d, d4 = d2 * d2, d8 = d4 * d4;
-                    nw = d8 * d4;
-                } else {
-                    nw = powf(d, p.phi_normal);
-                }
                 const float dl = nb.w - c_lum[k];
                 const float lsw = log_b3(dx < 0 ? -dx : dx) + log_b3(dy < 0 ? -dy : dy);
                 float t = fmaf(fabsf(cn[k].w - nd.w), a_d[k], lsw);
                 t = fmaf(dl * a_l[k], dl, t);
-                const float w = nw * ex2_approx(t);
+                float w;
+                if (kPow12) {
+                    // max(n.n', 0)^12 folded into the exponent: 2^(12 log2 d + t) (d = 0 gives 0)
+                    w = ex2_approx(fmaf(12.0f, lg2_approx(d), t));
+                } else {
+                    w = powf(d, p.phi_normal) * ex2_approx(t);
+                }
                 sr[k] = fmaf(nb.x, w, sr[k]);
                 sg[k] = fmaf(nb.y, w, sg[k]);
                 sb[k] = fmaf(nb.z, w, sb[k]);
