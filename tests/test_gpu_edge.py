@@ -92,6 +92,18 @@ def test_photon_debug_view(gpu, orc):
     assert match_frac(r.read_moments(), o.moments) >= FRAC
 
 
+@pytest.mark.parametrize("debug", [False, True])
+def test_photon_map_never_built(gpu, orc, debug):
+    """Photon gathering on with no rebuild: every lookup walks an empty grid (the reference reads its
+    zero-initialised buffers), paths still end at their first diffuse bounce."""
+    s = rt.Scene.cornell555()
+    cfg = rt.RenderConfig(width=32, height=24, spp=2, accumulate_frames=2, enable_denoise=False,
+                          enable_photon_map=True, photon_count=4096, photon_debug=debug)
+    r, o = render_both(orc, s, cfg, 2)
+    assert r.stats().photons_stored == 0
+    assert match_frac(r.read_accumulation(), o.accum) >= FRAC
+
+
 def test_accumulation_controls(gpu, orc):
     """reset_accumulation (hard and soft), update_lights, config mutation and sample_count."""
     s = rt.Scene.cornell555()
