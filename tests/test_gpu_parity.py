@@ -184,6 +184,19 @@ def test_photon_map_and_denoise_cornell(gpu, orc):
     assert f >= FRAC, f
 
 
+@pytest.mark.parametrize("grid_max_dim, radius_mode", [(26, 0), (130, 1), (130, 0)])
+def test_photon_gather_grid_modes(gpu, orc, grid_max_dim, radius_mode):
+    """The gather's photon lookups on an identical photon buffer, with the reference's grid (26 cells,
+    radius clamp(4 cell, .01, 2)), the fine grid with radius cell / 2, and the fine grid with the
+    reference's radius rule (a radius wider than the cell: every neighbour cell may hold hits)."""
+    scene = rt.Scene.cornell555()
+    cfg = rt.RenderConfig(width=48, height=40, spp=2, accumulate_frames=2, enable_denoise=False,
+                          enable_photon_map=True, photon_count=16384, photon_scale=2000.0,
+                          grid_max_dim=grid_max_dim, photon_radius_mode=radius_mode)
+    r, o = render_both(orc, scene, cfg, 2, photons=True)
+    assert match_frac(r.read_accumulation(), o.accum) >= FRAC
+
+
 def test_second_rebuild_counts_photons_left_from_the_first(gpu, orc):
     """The histogram is taken inside the photon pass; slots the second pass does not write keep the
     first pass's photons (the reference never clears the slot buffer) and must still be counted."""
