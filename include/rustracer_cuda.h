@@ -565,6 +565,14 @@ int rt_bvh_build(const float *centroids, const float *bbox_min, const float *bbo
 const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count);
 const uint32_t *rt_bvh_prims(const rt_bvh *b, uint64_t *count);
 void rt_bvh_destroy(rt_bvh *b);
+/* The four-wide traversal records of a tree in the reference's node layout (what scene upload builds
+ * under rt_set_traversal_width(4)): 32 floats per record, per child (min.xyz, ref) then
+ * (max.xyz, count) as bit patterns in the .w slots (count > 0: a leaf of `count` prim slots from
+ * `ref`; 0: an internal child, `ref` its record; 0xFFFFFFFF: an empty place).  Writes at most
+ * `capacity` floats to `out` (may be null to ask for the size); *records gets the record count and
+ * *stack_need the stack bound of a near-first walk. */
+int rt_bvh_wide_layout(const rt_bvh_node *nodes, uint64_t n_nodes, float *out, uint64_t capacity, uint64_t *records,
+                       uint32_t *stack_need);
 /* BVH builders (no counterpart in the reference, which builds on the host only): RT_BVH_HOST_SAH is
  * BVHBuilder::build (bvh.rs:135-336, the default); RT_BVH_GPU_LBVH builds a linear BVH on the GPU
  * (Morton codes of the centroids, one primitive per leaf) in the same node layout, falling back to

@@ -275,6 +275,7 @@ _PROTOS: dict[str, tuple] = {
     "rt_camera_zoom": (None, [P(Camera), C.c_float]),
     "rt_derive_grid": (None, [P(C.c_float), P(C.c_float), C.c_int, u32, u32, u32, P(GridParams), P(C.c_float)]),
     "rt_bvh_build": (C.c_int, [vp, vp, vp, C.c_uint64, P(vp)]),
+    "rt_bvh_wide_layout": (C.c_int, [vp, C.c_uint64, vp, C.c_uint64, P(C.c_uint64), P(u32)]),
     "rt_bvh_nodes": (P(BVHNode), [vp, P(C.c_uint64)]),
     "rt_bvh_prims": (P(C.c_uint32), [vp, P(C.c_uint64)]),
     "rt_bvh_destroy": (None, [vp]),

@@ -873,6 +873,21 @@ extern "C" int rt_bvh_build(const float *centroids, const float *bbox_min, const
     *out = b;
     return RT_OK;
 }
+extern "C" int rt_bvh_wide_layout(const rt_bvh_node *nodes, uint64_t n_nodes, float *out, uint64_t capacity,
+                                  uint64_t *records, uint32_t *stack_need) {
+    rt::clear_error();
+    if ((!nodes && n_nodes) || !records || !stack_need) {
+        rt::set_error("rt_bvh_wide_layout: null argument");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    rt::WideLayout w;
+    rt::build_wide_layout(nodes, n_nodes, w);
+    *records = w.nodes.size() / 32;
+    *stack_need = w.stack_need;
+    if (out) std::memcpy(out, w.nodes.data(), sizeof(float) * std::min<uint64_t>(capacity, w.nodes.size()));
+    return RT_OK;
+}
+
 extern "C" const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count) {
     if (count) *count = b ? b->b.nodes.size() : 0;
     return b ? b->b.nodes.data() : nullptr;

@@ -174,3 +174,53 @@ def test_threaded_build_equals_sequential_build():
     lib.rt_set_host_threads(0)
     assert out[0] == out[1] == out[2]
     assert len(out[0][1]) // 4 >= 20 * 4 ** 5  # large enough for threaded subtrees (8192 prims each)
+
+
+def wide_layout(nodes):
+    lib = A.load()
+    buf = np.ascontiguousarray(nodes)
+    recs, need = C.c_uint64(), C.c_uint32()
+    A.check("rt_bvh_wide_layout", lib.rt_bvh_wide_layout(buf.ctypes.data, len(buf), None, 0, C.byref(recs),
+                                                        C.byref(need)))
+    out = np.zeros(recs.value * 32, np.float32)
+    A.check("rt_bvh_wide_layout", lib.rt_bvh_wide_layout(buf.ctypes.data, len(buf), out.ctypes.data, out.size,
+                                                        C.byref(recs), C.byref(need)))
+    return out.reshape(-1, 4, 8), need.value
+
+
+@pytest.mark.parametrize("make", [lambda: rt.Scene.cornell555(),
+                                  lambda: rt.Scene.icosphere_room(level=4, seed=5, sigma=0.02, tex_size=0)])
+def test_wide_layout_is_the_same_tree(lib, make):
+    """The four-wide records hold every leaf of the reference's tree exactly once with its own box,
+    every record is reached exactly once, each record's children are the nodes it absorbed, and the
+    stack bound is the largest sum of (internal children - 1) along a root-to-leaf walk."""
+    nodes = make().arrays()["bvh_nodes"]
+    recs, need = wide_layout(nodes)
+    u = recs.view(np.uint32)
+    leaves = {(int(n["left_first"]), int(n["prim_count"])): n for n in nodes if n["prim_count"] > 0}
+    boxes = {tuple(n["bbox_min"]) + tuple(n["bbox_max"]) for n in nodes}
+    seen_rec = np.zeros(len(recs), np.int32)
+    seen_leaf = {}
+
+    def walk(r):  # the largest stack depth below record r
+        seen_rec[r] += 1
+        internal, deepest = 0, 0
+        for c in range(4):
+            ref, cnt = int(u[r, c, 3]), int(u[r, c, 7])
+            if cnt == 0xFFFFFFFF:
+                continue
+            box = tuple(recs[r, c, 0:3]) + tuple(recs[r, c, 4:7])
+            assert box in boxes  # every child box is a box of the reference's tree
+            if cnt > 0:
+                assert (ref, cnt) in leaves
+                seen_leaf[(ref, cnt)] = seen_leaf.get((ref, cnt), 0) + 1
+            else:
+                assert 0 < ref < len(recs)
+                internal += 1
+                deepest = max(deepest, walk(ref))
+        return internal - 1 + deepest if internal else 0
+
+    assert walk(0) == need
+    assert (seen_rec == 1).all()
+    assert seen_leaf == {k: 1 for k in leaves}
+    assert len(recs) < int((nodes["prim_count"] == 0).sum())  # fewer records than two-wide ones
