@@ -2,7 +2,8 @@
 // octrees, and k-d trees", HPG 2012) over the triangles' centroid Morton codes, written in the
 // reference's BVHNode layout (rustracer-core/src/bvh.rs:79-88) so that every consumer of the host
 // SAH build (BVHBuilder::build, bvh.rs:135-336) takes it unchanged.  It trades tree quality for build
-// time: one primitive per leaf, splits at Morton-code prefix changes instead of the SAH.
+// time: splits at Morton-code prefix changes instead of the SAH; subtrees of at most four primitives
+// are collapsed into leaves afterwards, the reference's leaf policy.
 //
 //   keys      (morton30(centroid) << 32) | prim: unique, so the sorted order (and the tree) is
 //             deterministic
@@ -10,7 +11,8 @@
 //   hierarchy one thread per internal node finds its key range and split (longest common prefix)
 //   boxes     one thread per leaf walks towards the root; at each node the second child to arrive
 //             (atomic counter) writes the union of the two children's boxes and continues
-//   depth     one thread per leaf counts its ancestors (the traversal stack must hold the depth)
+//   leaves    on the host: subtrees of at most four primitives become leaves (the reference's
+//             policy), and the tree is written root first with its depth measured
 //
 // Node numbering: internal nodes 0 .. n-2 (node 0 is the root), leaf of sorted position i is node
 // n-1+i with prims[i] its primitive.
@@ -148,25 +150,6 @@ __global__ void lbvh_boxes_kernel(const unsigned long long *__restrict__ keys, u
     }
 }
 
-// Ancestors of every leaf (the walk is bounded: a depth beyond 127 is reported as 128).
-__global__ void lbvh_depth_kernel(const uint32_t *__restrict__ parent, uint32_t n, uint32_t *max_depth) {
-    uint32_t best = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t node = n - 1u + i, d = 0;
-        while (node != 0u && d < 128u) {
-            node = parent[node];
-            ++d;
-            if (node >= n - 1u) {  // not an internal node: malformed input, report as too deep
-                d = 128u;
-                break;
-            }
-        }
-        best = max(best, d);
-    }
-    best = __reduce_max_sync(0xFFFFFFFFu, best);
-    if ((threadIdx.x & 31u) == 0u) atomicMax(max_depth, best);
-}
-
 struct Scratch {
     void *p = nullptr;
     ~Scratch() {
@@ -184,12 +167,12 @@ int build_lbvh(const float *centroids, const float *bmin, const float *bmax, uin
     uint32_t n_pad = 2048;
     while (n_pad < n) n_pad <<= 1;
     const size_t nodes = 2ull * n - 1ull;
-    // one allocation: keys, centroids, boxes, children, parent, arrivals, node boxes, depth
+    // one allocation: keys, centroids, boxes, children, parent, arrivals, node boxes
     const size_t off_keys = 0, off_c = off_keys + 8ull * n_pad, off_bmin = off_c + 12ull * n,
                  off_bmax = off_bmin + 12ull * n, off_child = (off_bmax + 12ull * n + 15) & ~15ull,
                  off_parent = off_child + 8ull * n, off_arr = off_parent + 4ull * nodes,
                  off_lo = (off_arr + 4ull * n + 15) & ~15ull, off_hi = off_lo + 16ull * nodes,
-                 off_depth = off_hi + 16ull * nodes, total = off_depth + 16;
+                 total = off_hi + 16ull * nodes;
     Scratch mem;
     if (cudaMalloc(&mem.p, total) != cudaSuccess) return -2;
     unsigned char *b = static_cast<unsigned char *>(mem.p);
@@ -202,7 +185,6 @@ int build_lbvh(const float *centroids, const float *bmin, const float *bmax, uin
     auto *arrivals = reinterpret_cast<uint32_t *>(b + off_arr);
     auto *nlo = reinterpret_cast<float4 *>(b + off_lo);
     auto *nhi = reinterpret_cast<float4 *>(b + off_hi);
-    auto *depth = reinterpret_cast<uint32_t *>(b + off_depth);
     // centroid bounds on the host (one pass) give the Morton grid
     float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
     for (uint32_t i = 0; i < n; ++i)
@@ -215,8 +197,7 @@ int build_lbvh(const float *centroids, const float *bmin, const float *bmax, uin
     if (cudaMemcpy(dc, centroids, 12ull * n, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(dlo_t, bmin, 12ull * n, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(dhi_t, bmax, 12ull * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(parent, 0xFF, 4ull * nodes) != cudaSuccess || cudaMemset(arrivals, 0, 4ull * n) != cudaSuccess ||
-        cudaMemset(depth, 0, 16) != cudaSuccess)
+        cudaMemset(parent, 0xFF, 4ull * nodes) != cudaSuccess || cudaMemset(arrivals, 0, 4ull * n) != cudaSuccess)
         return -2;
     const int sms = device_sm_count();
     auto grid = [&](uint64_t items) {
@@ -232,40 +213,82 @@ int build_lbvh(const float *centroids, const float *bmin, const float *bmax, uin
     }
     lbvh_internal_kernel<<<grid(n), 256>>>(keys, n, children, parent);
     lbvh_boxes_kernel<<<grid(n), 256>>>(keys, n, dlo_t, dhi_t, children, parent, arrivals, nlo, nhi);
-    lbvh_depth_kernel<<<grid(n), 256>>>(parent, n, depth);
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return -2;
     std::vector<unsigned long long> hkeys(n);
     std::vector<uint2> hchild(n - 1);
     std::vector<float4> hlo(nodes), hhi(nodes);
-    uint32_t hdepth = 0;
     if (cudaMemcpy(hkeys.data(), keys, 8ull * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(hchild.data(), children, 8ull * (n - 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(hlo.data(), nlo, 16ull * nodes, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hhi.data(), nhi, 16ull * nodes, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(&hdepth, depth, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        cudaMemcpy(hhi.data(), nhi, 16ull * nodes, cudaMemcpyDeviceToHost) != cudaSuccess)
         return -2;
-    if (max_depth) *max_depth = hdepth;
     out.prims.resize(n);
     for (uint32_t i = 0; i < n; ++i) out.prims[i] = (uint32_t)(hkeys[i] & 0xFFFFFFFFull);
-    out.nodes.resize(nodes);
-    for (size_t k = 0; k < nodes; ++k) {
-        rt_bvh_node &nd = out.nodes[k];
-        std::memset(&nd, 0, sizeof(nd));
-        nd.bbox_min[0] = hlo[k].x;
-        nd.bbox_min[1] = hlo[k].y;
-        nd.bbox_min[2] = hlo[k].z;
-        nd.bbox_max[0] = hhi[k].x;
-        nd.bbox_max[1] = hhi[k].y;
-        nd.bbox_max[2] = hhi[k].z;
-        if (k + 1 < n) {
-            nd.left_first = hchild[k].x;
-            nd.right_child = hchild[k].y;
-            nd.prim_count = 0;
-        } else {
-            nd.left_first = (uint32_t)(k - (n - 1));
-            nd.prim_count = 1;
+    // Leaf policy of BVHBuilder::build (bvh.rs:170-180): a subtree of at most max_prims_per_leaf (4)
+    // primitives becomes one leaf.  A subtree's primitives are a contiguous run of the sorted order,
+    // so its leaf covers prims[first, first + count).  Subtree sizes bottom-up (post-order walk).
+    constexpr uint32_t kMaxLeaf = 4;
+    std::vector<uint32_t> first(nodes), count(nodes);
+    for (uint32_t i = 0; i < n; ++i) {
+        first[n - 1 + i] = i;
+        count[n - 1 + i] = 1;
+    }
+    {
+        std::vector<std::pair<uint32_t, bool>> st;
+        st.push_back({0u, false});
+        while (!st.empty()) {
+            auto [k, done] = st.back();
+            st.pop_back();
+            if (k + 1 >= n) continue;  // a leaf
+            const uint32_t l = hchild[k].x, r = hchild[k].y;
+            if (!done) {
+                st.push_back({k, true});
+                st.push_back({r, false});
+                st.push_back({l, false});
+            } else {
+                first[k] = std::min(first[l], first[r]);
+                count[k] = count[l] + count[r];
+            }
         }
     }
+    // Emit in the reference's layout, root first, children numbered as they are reached.
+    out.nodes.clear();
+    out.nodes.reserve(nodes);
+    uint32_t deepest = 0;
+    struct Item {
+        uint32_t k, slot, depth;
+    };
+    std::vector<Item> st;
+    out.nodes.emplace_back();
+    st.push_back({0u, 0u, 0u});
+    while (!st.empty()) {
+        const Item it = st.back();
+        st.pop_back();
+        deepest = std::max(deepest, it.depth);
+        rt_bvh_node nd;
+        std::memset(&nd, 0, sizeof(nd));
+        nd.bbox_min[0] = hlo[it.k].x;
+        nd.bbox_min[1] = hlo[it.k].y;
+        nd.bbox_min[2] = hlo[it.k].z;
+        nd.bbox_max[0] = hhi[it.k].x;
+        nd.bbox_max[1] = hhi[it.k].y;
+        nd.bbox_max[2] = hhi[it.k].z;
+        if (count[it.k] <= kMaxLeaf) {
+            nd.left_first = first[it.k];
+            nd.prim_count = count[it.k];
+        } else {
+            const uint32_t l = (uint32_t)out.nodes.size();
+            out.nodes.emplace_back();
+            out.nodes.emplace_back();
+            nd.left_first = l;
+            nd.right_child = l + 1u;
+            nd.prim_count = 0;
+            st.push_back({hchild[it.k].y, l + 1u, it.depth + 1u});
+            st.push_back({hchild[it.k].x, l, it.depth + 1u});
+        }
+        out.nodes[it.slot] = nd;
+    }
+    if (max_depth) *max_depth = deepest;
     return 0;
 }
 

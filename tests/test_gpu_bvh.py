@@ -35,24 +35,39 @@ def test_lbvh_invariants(gpu, n):
     lo[: n // 10] = lo[0]  # duplicate centroids: equal Morton codes must still give a tree
     hi[: n // 10] = hi[0]
     nodes, prims, depth = gpu_build(lo, hi)
-    assert len(nodes) == 2 * n - 1 and sorted(prims.tolist()) == list(range(n))
+    assert len(nodes) <= 2 * n - 1 and sorted(prims.tolist()) == list(range(n))
     seen = np.zeros(n, np.int64)
-    stack, max_d = [(0, 0)], 0
-    while stack:
-        i, d = stack.pop()
-        max_d = max(max_d, d)
+    under = {}  # primitives below each node
+
+    def walk(i, d):
         nd = nodes[i]
         bmin, bmax = np.asarray(nd["bbox_min"]), np.asarray(nd["bbox_max"])
         if nd["prim_count"] > 0:
+            assert 1 <= nd["prim_count"] <= 4  # the reference's leaf size limit
             for k in range(nd["left_first"], nd["left_first"] + nd["prim_count"]):
                 p = prims[k]
                 seen[p] += 1
                 assert (bmin <= lo[p]).all() and (bmax >= hi[p]).all()
-        else:
-            for ch in (nd["left_first"], nd["right_child"]):
-                cmin, cmax = np.asarray(nodes[ch]["bbox_min"]), np.asarray(nodes[ch]["bbox_max"])
-                assert (bmin <= cmin).all() and (bmax >= cmax).all()
-                stack.append((ch, d + 1))
+            under[i] = int(nd["prim_count"])
+            return d
+        deepest = d
+        for ch in (nd["left_first"], nd["right_child"]):
+            cmin, cmax = np.asarray(nodes[ch]["bbox_min"]), np.asarray(nodes[ch]["bbox_max"])
+            assert (bmin <= cmin).all() and (bmax >= cmax).all()
+            stack.append((ch, d + 1))
+        return deepest
+
+    stack, max_d = [(0, 0)], 0
+    order = []
+    while stack:
+        i, d = stack.pop()
+        order.append(i)
+        max_d = max(max_d, walk(i, d))
+    for i in reversed(order):  # children were visited after their parents
+        nd = nodes[i]
+        if nd["prim_count"] == 0:
+            under[i] = under[int(nd["left_first"])] + under[int(nd["right_child"])]
+            assert under[i] > 4  # a subtree of at most four primitives is one leaf
     assert (seen == 1).all()
     assert depth == max_d
 
