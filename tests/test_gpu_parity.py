@@ -64,6 +64,32 @@ def test_cornell_config1_accumulation(gpu, orc):
     assert (np.abs(tm.astype(int) - o.output.astype(int)) <= 1).mean() >= FRAC
 
 
+def test_config1_error_against_a_converged_render(gpu, orc):
+    """The RMSE of config 1's 16-sample image against a converged (4096 spp) render is the same for the
+    CUDA path and the oracle, and it falls with more samples (the estimator converges to one image)."""
+    scene = rt.Scene.cornell555()
+    cam = scene.default_camera()
+
+    def gpu_image(spp, frames):
+        cfg = rt.RenderConfig(width=128, height=128, spp=spp, accumulate_frames=frames, enable_denoise=False)
+        r = rt.Renderer(scene, cfg)
+        r.update_camera(cam)
+        r.render_frames(frames)
+        img = r.read_accumulation()[..., :3].astype(np.float64)
+        r.close()
+        return img
+
+    converged = gpu_image(1, 4096)
+    cfg16 = rt.RenderConfig(width=128, height=128, spp=1, accumulate_frames=16, enable_denoise=False)
+    r, o = render_both(orc, scene, cfg16, 16)
+    rmse = lambda a: float(np.sqrt(np.mean((a - converged) ** 2)))  # noqa: E731
+    e_gpu = rmse(r.read_accumulation()[..., :3].astype(np.float64))
+    e_orc = rmse(o.accum[..., :3].astype(np.float64))
+    assert abs(e_gpu - e_orc) <= 0.01 * e_orc, (e_gpu, e_orc)
+    e_64 = rmse(gpu_image(1, 64))
+    assert e_64 < 0.7 * e_gpu, (e_64, e_gpu)  # ~1/sqrt(spp): 64 samples halve the error of 16
+
+
 def test_first_frame_buffers(gpu, orc):
     scene = rt.Scene.cornell555()
     cfg = rt.RenderConfig(width=128, height=96, spp=3, accumulate_frames=0, enable_denoise=False)
