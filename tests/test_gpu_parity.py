@@ -1,6 +1,6 @@
 """Parity of the sm_103a kernels (through the C ABI) with the oracle on the same inputs.
 
-Tolerances (floating point, written here as the benchmark spec states them):
+Tolerances (floating point, written here as the parity bar states them):
   * accumulated radiance: |gpu - oracle| <= 1e-3 |oracle| + 1e-6 on at least 99.9% of channels; the
     rest are paths that diverged on an ulp-level difference (CUDA's and glibc's sinf/cosf/powf/expf
     differ by an ulp or two, which can flip a silhouette hit or a lobe choice);
