@@ -599,6 +599,10 @@ void rt_set_host_threads(uint32_t n);
  * reference's closest hit; only triangles hit at exactly equal t may resolve to a different one of
  * them.  Returns RT_ERR_INVALID_ARGUMENT for other widths. */
 int rt_set_traversal_width(uint32_t width);
+/* Denoise blocks whose tensor-memory-accelerator tile copies did not arrive within the kernel's wait
+ * bound since the library was loaded (such a block writes nothing; 0 is the only expected value,
+ * 0xFFFFFFFF if the count cannot be read). */
+uint32_t rt_tma_timeouts(void);
 uint32_t rt_get_traversal_width(void);
 
 /* PNG scanline unfiltering for the glTF ingest (the reference decodes images through the `gltf` /

@@ -4,6 +4,9 @@
 //   denoise  rustracer-renderer/shaders/denoise.wgsl:122-195  (HBM-bound stencil: 64 B/px compulsory)
 //   resolve  rustracer-renderer/shaders/composite.wgsl:211-221 + tonemap.wgsl:240-271
 //            (streaming: frame 16 B + history 16 B read, history 16 B + rgba8 4 B written per pixel)
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "rt_kernels.h"
 
 namespace rtd {
@@ -101,6 +104,24 @@ __device__ __forceinline__ float lg2_approx(float x) {
     return r;
 }
 
+// Blocks whose tile copies did not arrive within the wait bound (none expected; read by
+// rt_tma_timeouts).
+__device__ unsigned int g_tma_timeouts = 0u;
+
+// Bounded wait for an mbarrier phase: true once it completed, false after 2^20 polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar_s, uint32_t phase) {
+    for (uint32_t i = 0; i < (1u << 20); ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(bar_s), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 template <int kStep, bool kInterior, bool kPow12>
 __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * kStep],
                                                const float4 (*s_nd)[kDnBX + 4 * kStep], const float *s_varc,
@@ -171,47 +192,50 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
 }
 
 template <int kStep>
-__global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(const float4 *__restrict__ in,
+__global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(const __grid_constant__ CUtensorMap tm_in,
+                                                                           const __grid_constant__ CUtensorMap tm_g,
                                                                            float4 *__restrict__ out,
-                                                                           const float4 *__restrict__ gbuffer,
                                                                            const float4 *__restrict__ moments,
                                                                            const rt_denoise_params p,
                                                                            const float *alpha_dev) {
     constexpr int H = 2 * kStep, TW = kDnBX + 2 * H, TH = kDnRows + 2 * H;
-    extern __shared__ float4 dn_smem[];
+    constexpr uint32_t kBox = 16u * TW * TH;  // bytes of one staged tile
+    extern __shared__ unsigned char dn_raw[];
+    // TMA writes the tiles at a 128-byte aligned shared address; the mbarrier follows the tiles.
+    float4 *dn_smem = reinterpret_cast<float4 *>(
+        (reinterpret_cast<uintptr_t>(dn_raw) + 127u) & ~static_cast<uintptr_t>(127u));
     float4(*s_cl)[TW] = reinterpret_cast<float4(*)[TW]>(dn_smem);
     float4(*s_nd)[TW] = reinterpret_cast<float4(*)[TW]>(dn_smem + TW * TH);
     float(*s_var)[kDnBX + 2] = reinterpret_cast<float(*)[kDnBX + 2]>(dn_smem + 2 * TW * TH);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(
+        reinterpret_cast<float *>(s_var) + ((kDnBX + 2) * (kDnRows + 2) + 1) / 2 * 2);
     const int W = (int)p.width, Hh = (int)p.height;
     const int tid = threadIdx.y * kDnBX + threadIdx.x;
     const int x0 = (int)blockIdx.x * kDnBX, y0t = (int)blockIdx.y * kDnRows;
     constexpr int kThreads = kDnBX * kDnThreadsY;
-    // Tile load: every load of this thread is issued before any shared-memory store, so a thread keeps
-    // up to 2 * kPer requests in flight instead of waiting on each in turn.
-    constexpr int kPer = (TW * TH + kThreads - 1) / kThreads;
-    {
-        float4 c[kPer], g[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            const int i = tid + k * kThreads;
-            const int ty = i / TW, tx = i - ty * TW;
-            const int gx = x0 - H + tx, gy = y0t - H + ty;
-            if (i < TW * TH && gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
-                const size_t q = (size_t)gy * W + gx;
-                c[k] = __ldg(in + q);
-                g[k] = __ldg(gbuffer + q);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            const int i = tid + k * kThreads;
-            const int ty = i / TW, tx = i - ty * TW;
-            const int gx = x0 - H + tx, gy = y0t - H + ty;
-            if (i < TW * TH && gx >= 0 && gy >= 0 && gx < W && gy < Hh) {
-                s_cl[ty][tx] = make_float4(c[k].x, c[k].y, c[k].z, luminance(mk3(c[k].x, c[k].y, c[k].z)));
-                s_nd[ty][tx] = g[k];
-            }
-        }
+    // Colour and G-buffer tiles (with the 2-step halo) staged by the tensor-memory accelerator: one
+    // thread arms the barrier with both tiles' bytes and issues the two copies (positions outside the
+    // image arrive as zeros and are never read: the taps check the image bounds) while the block
+    // loads the variance window.
+    const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s), "r"(2u * kBox) : "memory");
+        const int cx = x0 - H, cy = y0t - H;
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(&s_cl[0][0])),
+            "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(&s_nd[0][0])),
+            "l"(reinterpret_cast<uint64_t>(&tm_g)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
+            : "memory");
     }
     constexpr int kVarN = (kDnBX + 2) * (kDnRows + 2);
     constexpr int kVarPer = (kVarN + kThreads - 1) / kThreads;
@@ -235,6 +259,20 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
             // -1 marks a position outside the image
             s_var[ty][tx] = (gx >= 0 && gy >= 0 && gx < W && gy < Hh) ? fmaxf(m[k].y - m[k].x * m[k].x, 0.0f) : -1.0f;
         }
+    }
+    // Wait for the two tiles (phase 0 of the barrier), bounded: a block whose copies do not arrive
+    // counts the fault, waits once more (bounded) for them and leaves without writing.
+    if (__syncthreads_or(!mbar_wait(bar_s, 0u)) != 0) {
+        if (tid == 0) {
+            atomicAdd(&g_tma_timeouts, 1u);
+            mbar_wait(bar_s, 0u);
+        }
+        return;
+    }
+    // The colour tile's fourth channel becomes the luminance the taps compare.
+    for (int i = tid; i < TW * TH; i += kThreads) {
+        float4 &c = (&s_cl[0][0])[i];
+        c.w = luminance(mk3(c.x, c.y, c.z));
     }
     __syncthreads();
     // This thread's column: rows r0 + k*step of the tile, k = 0..3.
@@ -284,7 +322,9 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
 
 template <int kStep>
 constexpr size_t denoise_smem_bytes() {
-    return sizeof(float4) * 2 * (kDnBX + 4 * kStep) * (kDnRows + 4 * kStep) + sizeof(float) * (kDnBX + 2) * (kDnRows + 2);
+    // 128 bytes of alignment slack, the two tiles, the variance window (rounded to 8 bytes), the barrier
+    return 128 + sizeof(float4) * 2 * (kDnBX + 4 * kStep) * (kDnRows + 4 * kStep) +
+           sizeof(float) * (((kDnBX + 2) * (kDnRows + 2) + 1) / 2 * 2) + 8;
 }
 
 void prepare_kernels() {
@@ -298,16 +338,60 @@ void prepare_kernels() {
     done = true;
 }
 
+namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// A W x H image of float4 (16-byte rows of 4 floats, row pitch 16 W bytes) as a 3-D tensor
+// (channel, x, y) copied in side x side pixel boxes; positions outside the image read as zeros.
+cudaError_t encode_tile_map(CUtensorMap *tm, const float4 *base, uint32_t w, uint32_t h, uint32_t side) {
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const cuuint64_t dims[3] = {4u, w, h};
+    const cuuint64_t strides[2] = {16u, 16ull * w};
+    const cuuint32_t box[3] = {4u, side, side};
+    const cuuint32_t elem[3] = {1u, 1u, 1u};
+    const CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float4 *>(base), dims, strides, box,
+                              elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+uint32_t tma_timeouts() {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tma_timeouts, sizeof(v)) != cudaSuccess) return 0xFFFFFFFFu;
+    return v;
+}
+
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
                            const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st) {
     if (p.step_size == 1u || p.step_size == 2u) {
         prepare_kernels();
         dim3 block(kDnBX, kDnThreadsY);
         dim3 grid((p.width + kDnBX - 1) / kDnBX, (p.height + kDnRows - 1) / kDnRows);
+        const uint32_t side = (uint32_t)(kDnBX + 4 * p.step_size);
+        CUtensorMap tm_in, tm_g;
+        cudaError_t e;
+        if ((e = encode_tile_map(&tm_in, in, p.width, p.height, side)) != cudaSuccess) return e;
+        if ((e = encode_tile_map(&tm_g, gbuffer, p.width, p.height, side)) != cudaSuccess) return e;
         if (p.step_size == 1u)
-            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(in, out, gbuffer, moments, p, alpha_dev);
+            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(tm_in, tm_g, out, moments, p, alpha_dev);
         else
-            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(in, out, gbuffer, moments, p, alpha_dev);
+            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(tm_in, tm_g, out, moments, p, alpha_dev);
         return cudaGetLastError();
     }
     dim3 block(32, 8);

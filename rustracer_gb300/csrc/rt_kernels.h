@@ -128,6 +128,8 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st);
 // Image kernels.
 // alpha_dev, when not null, is read on the device in place of p.alpha (a CUDA graph replays the
 // launch with the value of the frame being replayed).
+// Denoise blocks whose TMA tile copies missed the wait bound since the library loaded (0 expected).
+uint32_t tma_timeouts();
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
                            const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st);
 // accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass; alpha_dev as above.

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import rustracer_gb300 as rt
+from rustracer_gb300 import _abi as A
 
 pytestmark = pytest.mark.gpu
 
@@ -130,6 +131,11 @@ def test_denoise_stage(gpu, orc, h, w):
             g = rt.stage_denoise(frame, gbuf, mom, alpha, passes)
             ref = orc.denoise(frame, gbuf, mom, alpha, passes)
             assert match_frac(g, ref, rtol=1e-5, atol=1e-7) == 1.0
+
+
+def test_denoise_tiles_arrive(gpu):
+    """Every denoise block of the tests so far received its TMA tile copies within the wait bound."""
+    assert A.load().rt_tma_timeouts() == 0
 
 
 def test_resolve_stage(gpu, orc):
