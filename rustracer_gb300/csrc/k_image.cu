@@ -419,7 +419,9 @@ __global__ void __launch_bounds__(256) resolve_kernel(const float4 *__restrict__
     const f3 exposed = mk3(h.x, h.y, h.z) * tp.exposure;
     const f3 mapped = exposed / (exposed + mk3(1.0f, 1.0f, 1.0f));
     const float ig = 1.0f / tp.gamma;
-    f3 color = mk3(powf(mapped.x, ig), powf(mapped.y, ig), powf(mapped.z, ig));
+    // pow(mapped, 1/gamma) for mapped in [0, 1): the hardware exp2 / log2 form (the rgba8 result is
+    // within one step of the correctly rounded pow, as the tonemap of the reference's backend is)
+    f3 color = mk3(__powf(mapped.x, ig), __powf(mapped.y, ig), __powf(mapped.z, ig));
     if (tp.marker[3] > 0.0f) {
         const uint32_t x = i % width, y = i / width;
         float ddx = ((float)x + 0.5f) - tp.marker[0], ddy = ((float)y + 0.5f) - tp.marker[1];
