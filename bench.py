@@ -301,11 +301,11 @@ def photon_denoise_stages(steps: int, warmup: int, peak: float) -> dict:
     npix = cfg.width * cfg.height
     t_ms, g_ms = statistics.median(trace_ms), statistics.median(grid_ms)
     # Compulsory bytes of this dataflow (the photon pass emits u32 keys): keys read by the count and
-    # the scatter (4 + 4 B/slot); counts read twice by the scan and (start, count) written (16 B/cell);
-    # per binned photon the rank written by the count and read by the scatter (4 + 4), the slot order
-    # written by the scatter, read and written by the per-cell order pass and read by the gather
-    # (4 + 4 + 4 + 4), the 64 B photon read + 64 B write of the gather and its 16 B compact position.
-    grid_bytes = 8.0 * slots + 16.0 * cells + (8.0 + 16.0 + 128.0 + 16.0) * binned
+    # the scatter (4 + 4 B/slot); counts read once by the single-pass scan and (start, count) written
+    # (12 B/cell); per binned photon the rank written by the count and read by the scatter (4 + 4), the
+    # slot order written by the scatter and read by the per-cell sort-and-copy pass (4 + 4), the 64 B
+    # photon read + 64 B write of that pass and its 16 B compact position.
+    grid_bytes = 8.0 * slots + 12.0 * cells + (8.0 + 8.0 + 128.0 + 16.0) * binned
     den_bytes = 2 * 64.0 * npix
     res_bytes = 52.0 * npix
     r.close()

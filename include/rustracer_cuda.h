@@ -603,6 +603,11 @@ int rt_set_traversal_width(uint32_t width);
  * bound since the library was loaded (such a block writes nothing; 0 is the only expected value,
  * 0xFFFFFFFF if the count cannot be read). */
 uint32_t rt_tma_timeouts(void);
+/* Photon-grid scans whose look-back for a preceding tile's sum gave up at the kernel's wait bound
+ * since the library was loaded (such a grid's offsets are wrong; 0 is the only expected value,
+ * 0xFFFFFFFF if the count cannot be read).  The scan replaces the host scan of
+ * rustracer-renderer/src/lib.rs:956-1007. */
+uint32_t rt_scan_timeouts(void);
 uint32_t rt_get_traversal_width(void);
 
 /* PNG scanline unfiltering for the glTF ingest (the reference decodes images through the `gltf` /

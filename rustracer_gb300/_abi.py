@@ -227,6 +227,7 @@ _PROTOS: dict[str, tuple] = {
     "rt_set_traversal_width": (C.c_int, [u32]),
     "rt_get_traversal_width": (u32, []),
     "rt_tma_timeouts": (u32, []),
+    "rt_scan_timeouts": (u32, []),
     "rt_scene_set_bvh_builder": (C.c_int, [vp, u32]),
     "rt_scene_bvh_builder_used": (u32, [vp]),
     "rt_bvh_build_gpu": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float), u64, P(vp), P(u32)]),

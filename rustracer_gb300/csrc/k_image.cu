@@ -98,6 +98,11 @@ __device__ __forceinline__ float ex2_approx(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ float lg2_approx(float x) {
     float r;
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -135,8 +140,8 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
     for (int k = 0; k < kDnPix; ++k) {
         c_lum[k] = s_cl[ly0 + H + k * kStep][lx + H].w;
         cn[k] = s_nd[ly0 + H + k * kStep][lx + H];
-        a_l[k] = -kLog2e * __frcp_rn(s_varc[k] * p.lambda + 1e-6f);
-        a_d[k] = -kLog2e * __frcp_rn(p.phi_depth * fmaxf(cn[k].w, 1e-4f));
+        a_l[k] = -kLog2e * rcp_approx(s_varc[k] * p.lambda + 1e-6f);
+        a_d[k] = -kLog2e * rcp_approx(p.phi_depth * fmaxf(cn[k].w, 1e-4f));
         sr[k] = sg[k] = sb[k] = tot[k] = 0.0f;
     }
     // Tap rows j = 0 .. 7 (row offset (j - 2) * step from the first pixel); pixel k uses rows k .. k+4.
@@ -182,7 +187,7 @@ __device__ __forceinline__ void denoise_column(const float4 (*s_cl)[kDnBX + 4 * 
         if (!kInterior && (x >= W || y >= Hh)) continue;
         const size_t idx = (size_t)y * W + x;
         if (tot[k] > 1e-6f) {
-            const float inv = __frcp_rn(tot[k]);
+            const float inv = rcp_approx(tot[k]);
             out[idx] = make_float4(sr[k] * inv, sg[k] * inv, sb[k] * inv, 1.0f);
         } else {
             const float4 c = s_cl[ly0 + H + k * kStep][lx + H];
@@ -237,28 +242,28 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
             "l"(reinterpret_cast<uint64_t>(&tm_g)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
             : "memory");
     }
-    constexpr int kVarN = (kDnBX + 2) * (kDnRows + 2);
-    constexpr int kVarPer = (kVarN + kThreads - 1) / kThreads;
+    // Variance window ((32 + 2) x (32 + 2), -1 outside the image): columns 0..31 at rows
+    // threadIdx.y + 8 k, and the last two columns one value each for threads 0..67.
     {
-        float2 m[kVarPer];
+        constexpr int VW = kDnBX + 2, VH = kDnRows + 2, kRowsPer = (VH + kDnThreadsY - 1) / kDnThreadsY;
+        const int tx = (int)threadIdx.x;
+        auto inside = [&](int gx, int gy) { return gx >= 0 && gy >= 0 && gx < W && gy < Hh; };
+        float2 m[kRowsPer], me = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int k = 0; k < kVarPer; ++k) {
-            const int i = tid + k * kThreads;
-            const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
-            const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
+        for (int k = 0; k < kRowsPer; ++k) {
+            const int vy = (int)threadIdx.y + k * kDnThreadsY, gx = x0 - 1 + tx, gy = y0t - 1 + vy;
             m[k] = make_float2(0.0f, 0.0f);
-            if (i < kVarN && gx >= 0 && gy >= 0 && gx < W && gy < Hh)
-                m[k] = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
+            if (vy < VH && inside(gx, gy)) m[k] = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)gy * W + gx));
         }
+        const int ey = tid >> 1, ex = kDnBX + (tid & 1), egx = x0 - 1 + ex, egy = y0t - 1 + ey;
+        if (tid < 2 * VH && inside(egx, egy))
+            me = __ldg(reinterpret_cast<const float2 *>(moments + (size_t)egy * W + egx));
 #pragma unroll
-        for (int k = 0; k < kVarPer; ++k) {
-            const int i = tid + k * kThreads;
-            if (i >= kVarN) continue;
-            const int ty = i / (kDnBX + 2), tx = i - ty * (kDnBX + 2);
-            const int gx = x0 - 1 + tx, gy = y0t - 1 + ty;
-            // -1 marks a position outside the image
-            s_var[ty][tx] = (gx >= 0 && gy >= 0 && gx < W && gy < Hh) ? fmaxf(m[k].y - m[k].x * m[k].x, 0.0f) : -1.0f;
+        for (int k = 0; k < kRowsPer; ++k) {
+            const int vy = (int)threadIdx.y + k * kDnThreadsY, gx = x0 - 1 + tx, gy = y0t - 1 + vy;
+            if (vy < VH) s_var[vy][tx] = inside(gx, gy) ? fmaxf(m[k].y - m[k].x * m[k].x, 0.0f) : -1.0f;
         }
+        if (tid < 2 * VH) s_var[ey][ex] = inside(egx, egy) ? fmaxf(me.y - me.x * me.x, 0.0f) : -1.0f;
     }
     // Wait for the two tiles (phase 0 of the barrier), bounded: a block whose copies do not arrive
     // counts the fault, waits once more (bounded) for them and leaves without writing.
@@ -281,7 +286,9 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
     const int lx = (int)threadIdx.x, x = x0 + lx, y0 = y0t + r0;
     const float alpha = alpha_dev ? *alpha_dev : p.alpha;
     const float ema_scale = alpha / fmaxf(2.0f - alpha, 1e-4f);
-    const bool interior = x0 - H >= 0 && y0t - H >= 0 && x0 + kDnBX + H <= W && y0t + kDnRows + H <= Hh;
+    // Warps whose every tap and 3 x 3 window lies inside the image skip the bounds tests.
+    const bool interior = __all_sync(0xFFFFFFFFu, x - H >= 0 && x + H < W && y0 - H >= 0 &&
+                                                      y0 + (kDnPix - 1) * kStep + H < Hh);
     float varc[kDnPix];
     if (interior) {
         // every 3 x 3 window is inside the image: sums of three per tile row, shared by the

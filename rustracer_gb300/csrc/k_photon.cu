@@ -15,6 +15,11 @@
 //                         slot order, independent of atomic arrival order (the reference's order
 //                         within a cell is unspecified)
 //     gather_kernel       sorted[i] = photons[order[i]] (64-byte records)
+//   grid build with ranks (the renderer's path): count_rank (histogram + each slot's rank in atomic
+//   order), scan_lookback_list (single-pass scan + list of occupied cells), scatter_rank (start + rank,
+//   no atomics), then cell_gather: per occupied cell the slot order restored and the records copied
+//   in one pass.
+#include <algorithm>
 #include <cstring>
 
 #include "rt_kernels.h"
@@ -747,21 +752,27 @@ __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__rest
 // Histogram with ranks: counts[key] += 1 and rank[slot] = the count found before the add (the slot's
 // position within its cell, in atomic order).
 __global__ void __launch_bounds__(256) count_rank_kernel(const uint32_t *__restrict__ keys, uint64_t n,
-                                                         uint32_t *__restrict__ counts, uint32_t *__restrict__ rank) {
-    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+                                                         uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
+                                                         uint32_t *__restrict__ clear, uint32_t n_clear) {
+    // the scan's chunk status words and ticket start at zero (this launch precedes the scan)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_clear; i += gridDim.x * blockDim.x) clear[i] = 0u;
+    // eight keys per thread and pass (two 16-byte loads in flight), then the adds, then the ranks
+    const uint64_t stride = 8ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t half = 4ull * gridDim.x * blockDim.x;
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
-        const uint64_t s0 = start + r * stride;
-        const uint4 k4 = load_keys4(keys, s0, n);
-        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-        uint32_t rk[4];
+        const uint64_t s0 = start + r * stride, s1 = s0 + half;
+        const uint4 a = load_keys4(keys, s0, n);
+        const uint4 b = load_keys4(keys, s1, n);
+        const uint32_t kk[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t rk[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 8; ++j)
             if (kk[j] != kInvalidKey) rk[j] = atomicAdd(counts + kk[j], 1u);
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (kk[j] != kInvalidKey) rank[s0 + j] = rk[j];
+        for (int j = 0; j < 8; ++j)
+            if (kk[j] != kInvalidKey) rank[(j < 4 ? s0 : s1) + (j & 3)] = rk[j];
     }
 }
 
@@ -822,25 +833,280 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_list_kernel(const uin
         if (v[i]) list[wbase++] = base + i;
 }
 
+// Single-pass exclusive scan of counts into (start, count) with decoupled look-back (Merrill and
+// Garland, "Single-pass Parallel Prefix Scan with Decoupled Look-back", 2016), plus the list of
+// occupied cells.  Each block owns a chunk of CT consecutive tiles of kScanTile cells: it loads and
+// sums the chunk's counts (kept in registers), publishes one status word -- flag in bits 30-31 (1: the chunk's own sum,
+// 2: the sum of all chunks up to and including it), value in bits 0-29 -- and warp 0 reads back 32
+// predecessors at a time until it meets an inclusive sum; then the block scans its tiles with that
+// prefix and writes (start, count).  Chunks are numbered by a ticket
+// taken when the block starts, so every chunk a block waits on belongs to a block already running:
+// the waits end.  They are bounded all the same (2^20 polls, then the block counts the timeout in
+// g_scan_timeouts and uses the sums it has).  Values must stay below 2^30 (the host checks the slot
+// count).
+constexpr uint32_t kScanFlagAgg = 1u << 30, kScanFlagIncl = 2u << 30, kScanValMask = (1u << 30) - 1u;
+__device__ unsigned int g_scan_timeouts = 0u;
+
+__device__ __forceinline__ void load_counts8(const uint32_t *__restrict__ counts, uint32_t base, uint32_t n, bool vec,
+                                             uint32_t (&v)[kScanItems]) {
+    if (vec && base + kScanItems <= n) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(counts + base));
+        const uint4 b = __ldg(reinterpret_cast<const uint4 *>(counts + base + 4));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? __ldg(counts + base + i) : 0u;
+    }
+}
+
+template <int CT>
+__global__ void __launch_bounds__(kScanThreads) scan_lookback_list_kernel(const uint32_t *__restrict__ counts,
+                                                                          uint32_t n, uint32_t *status,
+                                                                          uint32_t chunks, uint2 *__restrict__ meta,
+                                                                          bool vec, uint32_t *__restrict__ list,
+                                                                          uint32_t *__restrict__ n_list,
+                                                                          uint32_t *__restrict__ total_out) {
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    __shared__ uint32_t s_chunk, s_prefix;
+    if (threadIdx.x == 0) s_chunk = atomicAdd(status + chunks, 1u);
+    __syncthreads();
+    const uint32_t chunk = s_chunk;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tile0 = chunk * CT;
+    // the chunk's counts (all loads in flight at once, kept for the rescan) and their sum
+    uint32_t v[CT][kScanItems];
+#pragma unroll
+    for (int t = 0; t < CT; ++t) load_counts8(counts, (tile0 + t) * kScanTile + threadIdx.x * kScanItems, n, vec, v[t]);
+    uint32_t part = 0;
+#pragma unroll
+    for (int t = 0; t < CT; ++t)
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) part += v[t][i];
+    part = __reduce_add_sync(0xFFFFFFFFu, part);
+    if (lane == 0u) warp_sums[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x < 32u) {
+        uint32_t chunk_total = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
+        chunk_total = __reduce_add_sync(0xFFFFFFFFu, chunk_total);
+        volatile uint32_t *vs = status;
+        uint32_t prefix = 0;
+        if (chunk == 0u) {
+            if (lane == 0u) vs[0] = kScanFlagIncl | chunk_total;
+        } else {
+            if (lane == 0u) vs[chunk] = kScanFlagAgg | chunk_total;
+            int64_t window = (int64_t)chunk - 1;  // predecessor read by lane 0
+            uint32_t polls = 0;
+            bool timed_out = false;
+            for (;;) {
+                const int64_t idx = window - (int64_t)lane;
+                uint32_t sw = kScanFlagIncl;
+                if (idx >= 0) sw = vs[idx];
+                while (__any_sync(0xFFFFFFFFu, (sw >> 30) == 0u)) {
+                    if (++polls >= (1u << 20)) {
+                        timed_out = true;
+                        break;
+                    }
+                    if ((sw >> 30) == 0u) sw = vs[idx];
+                }
+                if (timed_out) break;
+                const uint32_t incl = __ballot_sync(0xFFFFFFFFu, (sw >> 30) == 2u);
+                // lanes up to the nearest inclusive predecessor (lowest lane) contribute
+                const uint32_t upto = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
+                prefix += __reduce_add_sync(0xFFFFFFFFu, lane <= upto ? (sw & kScanValMask) : 0u);
+                if (incl) break;
+                window -= 32;
+            }
+            if (timed_out && lane == 0u) atomicAdd(&g_scan_timeouts, 1u);
+            if (lane == 0u) vs[chunk] = kScanFlagIncl | ((prefix + chunk_total) & kScanValMask);
+        }
+        if (lane == 0u) {
+            s_prefix = prefix;
+            if (chunk == chunks - 1u && total_out) *total_out = prefix + chunk_total;
+        }
+    }
+    __syncthreads();
+    uint32_t carry = s_prefix;
+#pragma unroll
+    for (int t = 0; t < CT; ++t) {
+        const uint32_t base = (tile0 + t) * kScanTile + threadIdx.x * kScanItems;
+        uint32_t local = 0, occ = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) {
+            local += v[t][i];
+            occ += v[t][i] ? 1u : 0u;
+        }
+        uint32_t tile_total = 0;
+        uint32_t ex = block_exclusive_scan(local, warp_sums, &tile_total) + carry;
+        carry += tile_total;
+        uint32_t st[kScanItems];
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) {
+            st[i] = ex;
+            ex += v[t][i];
+        }
+        if (vec && base + kScanItems <= n) {
+            uint4 *m4 = reinterpret_cast<uint4 *>(meta + base);
+#pragma unroll
+            for (uint32_t i = 0; i < kScanItems; i += 2)
+                m4[i / 2] = make_uint4(st[i], v[t][i], st[i + 1], v[t][i + 1]);
+        } else {
+#pragma unroll
+            for (uint32_t i = 0; i < kScanItems; ++i)
+                if (base + i < n) meta[base + i] = make_uint2(st[i], v[t][i]);
+        }
+        // warp-exclusive offsets of the occupied cells, one atomic per warp
+        uint32_t x = occ;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        const uint32_t warp_total = __shfl_sync(0xFFFFFFFFu, x, 31);
+        uint32_t wbase = 0;
+        if (lane == 0u && warp_total) wbase = atomicAdd(n_list, warp_total);
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0) + x - occ;
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i)
+            if (v[t][i]) list[wbase++] = base + i;
+        __syncthreads();  // warp_sums is reused by the next tile's scan
+    }
+}
+
+uint32_t scan_timeouts() {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_scan_timeouts, sizeof(v)) != cudaSuccess) return 0xFFFFFFFFu;
+    return v;
+}
+
 // order[start[key] + rank[slot]] = slot: positions come from the ranks, no atomics.
 __global__ void __launch_bounds__(256) scatter_rank_kernel(const uint32_t *__restrict__ keys,
                                                            const uint32_t *__restrict__ rank, uint64_t n,
                                                            const uint2 *__restrict__ meta,
                                                            uint32_t *__restrict__ order) {
-    const uint64_t stride = 4ull * gridDim.x * blockDim.x;
+    // eight keys per thread and pass (two 16-byte loads in flight), then the starts and ranks, then the
+    // stores
+    const uint64_t stride = 8ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    const uint64_t half = 4ull * gridDim.x * blockDim.x;
     const uint64_t rounds = (n + stride - 1) / stride;
     for (uint64_t r = 0; r < rounds; ++r) {
-        const uint64_t s0 = start + r * stride;
-        const uint4 k4 = load_keys4(keys, s0, n);
-        const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-        uint32_t pos[4];
+        const uint64_t s0 = start + r * stride, s1 = s0 + half;
+        const uint4 a = load_keys4(keys, s0, n);
+        const uint4 b = load_keys4(keys, s1, n);
+        const uint32_t kk[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t pos[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (kk[j] != kInvalidKey) pos[j] = __ldg(&meta[kk[j]].x) + __ldg(rank + s0 + j);
+        for (int j = 0; j < 8; ++j)
+            if (kk[j] != kInvalidKey) pos[j] = __ldg(&meta[kk[j]].x) + __ldg(rank + (j < 4 ? s0 : s1) + (j & 3));
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)(s0 + j);
+        for (int j = 0; j < 8; ++j)
+            if (kk[j] != kInvalidKey) order[pos[j]] = (uint32_t)((j < 4 ? s0 : s1) + (j & 3));
+    }
+}
+
+// Copies photon records order-sorted: sorted[dst] = photons[slot] (64 B) and sorted_pos[dst] = its first
+// float4.  Two records per call with both loads issued before the stores.
+__device__ __forceinline__ void copy_photon_pair(const float4 *__restrict__ photons, uint32_t s0, uint32_t s1, bool two,
+                                                 float4 *__restrict__ sorted, float4 *__restrict__ sorted_pos,
+                                                 uint64_t d0, uint64_t d1, bool wide) {
+    if (wide) {
+        Photon8 a, b;
+        load_photon_wide(photons + 4ull * s0, a);
+        if (two) load_photon_wide(photons + 4ull * s1, b);
+        store_photon_wide(sorted + 4ull * d0, a);
+        if (sorted_pos) sorted_pos[d0] = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+        if (two) {
+            store_photon_wide(sorted + 4ull * d1, b);
+            if (sorted_pos) sorted_pos[d1] = make_float4(b.v[0], b.v[1], b.v[2], b.v[3]);
+        }
+    } else {
+        const float4 *p0 = photons + 4ull * s0, *p1 = photons + 4ull * (two ? s1 : s0);
+        const float4 a = __ldg(p0), b = __ldg(p0 + 1), c = __ldg(p0 + 2), d = __ldg(p0 + 3);
+        const float4 e = __ldg(p1), f = __ldg(p1 + 1), g = __ldg(p1 + 2), h = __ldg(p1 + 3);
+        float4 *q0 = sorted + 4ull * d0;
+        q0[0] = a;
+        q0[1] = b;
+        q0[2] = c;
+        q0[3] = d;
+        if (sorted_pos) sorted_pos[d0] = a;
+        if (two) {
+            float4 *q1 = sorted + 4ull * d1;
+            q1[0] = e;
+            q1[1] = f;
+            q1[2] = g;
+            q1[3] = h;
+            if (sorted_pos) sorted_pos[d1] = e;
+        }
+    }
+}
+
+// Copies a cell's records in slot order: sorted[start + i] = photons[src[i]], i < count, two records
+// per lane and round (lanes i and i + 32).
+__device__ __forceinline__ void copy_cell(const uint32_t *src, uint32_t start, uint32_t count, uint32_t lane,
+                                          const float4 *__restrict__ photons, float4 *__restrict__ sorted,
+                                          float4 *__restrict__ sorted_pos, bool wide) {
+    for (uint32_t i = lane; i < count; i += 64) {
+        const bool two = i + 32 < count;
+        copy_photon_pair(photons, src[i], two ? src[i + 32] : 0u, two, sorted, sorted_pos, (uint64_t)start + i,
+                         (uint64_t)start + i + 32, wide);
+    }
+}
+
+// The slot indices of one cell of at most 32 R photons (atomic order, from the scatter) sorted
+// ascending in registers into the warp's shared buffer.
+template <int R>
+__device__ __forceinline__ void sort_cell_to(const uint32_t *__restrict__ order, uint32_t start, uint32_t count,
+                                             uint32_t lane, uint32_t *buf) {
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = lane * R + r;
+        v[r] = e < count ? __ldg(order + start + e) : 0xFFFFFFFFu;
+    }
+    if (count > 1u) warp_sort_regs<R>(v, lane);
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[lane * R + r] = v[r];
+}
+
+constexpr uint32_t kCellRegsMax = 256;  // cells up to this size are sorted in registers
+
+// Per-cell slot order fused with the photon gather: one warp per listed (occupied) cell sorts the
+// cell's slot indices ascending -- photons of a cell keep slot order, as a sequential scatter would
+// leave them -- and copies the cell's records into sorted order.  Cells of more than 256 photons are
+// sorted in place in `order`, then copied from there.
+__global__ void __launch_bounds__(kOrderWarps * 32, 4) cell_gather_kernel(const uint2 *__restrict__ meta,
+                                                                       const uint32_t *__restrict__ list,
+                                                                       const uint32_t *__restrict__ n_list,
+                                                                       uint32_t *__restrict__ order,
+                                                                       const float4 *__restrict__ photons,
+                                                                       float4 *__restrict__ sorted,
+                                                                       float4 *__restrict__ sorted_pos, bool wide) {
+    __shared__ uint32_t sbuf[kOrderWarps][kCellRegsMax];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t *buf = sbuf[w];
+    const uint32_t warps_total = gridDim.x * kOrderWarps;
+    const uint32_t n = *n_list;
+    for (uint32_t li = blockIdx.x * kOrderWarps + w; li < n; li += warps_total) {
+        const uint2 m = __ldg(meta + __ldg(list + li));
+        const uint32_t start = m.x, count = m.y;
+        if (count == 0u) continue;
+        const uint32_t *src = buf;
+        if (count <= 32u) {
+            sort_cell_to<1>(order, start, count, lane, buf);
+        } else if (count <= 64u) {
+            sort_cell_to<2>(order, start, count, lane, buf);
+        } else if (count <= 128u) {
+            sort_cell_to<4>(order, start, count, lane, buf);
+        } else if (count <= kCellRegsMax) {
+            sort_cell_to<8>(order, start, count, lane, buf);
+        } else {
+            warp_bitonic(order + start, count, lane);
+            src = order + start;
+        }
+        __syncwarp();
+        copy_cell(src, start, count, lane, photons, sorted, sorted_pos, wide);
+        __syncwarp();
     }
 }
 
@@ -863,17 +1129,40 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
         // The occupied cells are listed in the cursor array (no cursors are needed with ranks); the
         // list length is total[1].
         if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-        if (n) count_rank_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank);
-        scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
-        scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
-        scan_apply_list_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec, g.cursor,
-                                                               g.total + 1);
+        // One scan pass with decoupled look-back while every value fits its 30 bits, else the three
+        // phases.  Chunks of up to four tiles, about two chunks per SM; the look-back's chunk status
+        // words and ticket (scan_partials[0 .. chunks], chunks <= tiles) are cleared by the count
+        // launch (or by a memset when there are no slots to count).
+        const bool lookback = n < (uint64_t)kScanValMask;
+        const uint32_t want = (tiles + 2 * sm - 1) / (2 * sm);
+        const uint32_t ct = want <= 1u ? 1u : (want <= 2u ? 2u : 4u);
+        const uint32_t chunks = (tiles + ct - 1) / ct;
         if (n) {
-            scatter_rank_kernel<<<grid_for((n + 3) / 4, 256, 8), 256, 0, st>>>(g.keys, g.rank, n, g.meta, g.order);
-            order_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 8), kOrderWarps * 32, 0, st>>>(
-                g.meta, g.cursor, g.total + 1, g.order);
-            photon_gather_kernel<<<grid_for((n + 1) / 2, 256, 8), 256, 0, st>>>(g.photons, g.order, g.total, n,
-                                                                                  g.sorted, g.sorted_pos, wide);
+            count_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank,
+                                                                             g.scan_partials, lookback ? chunks + 1 : 0u);
+        } else if ((e = cudaMemsetAsync(g.scan_partials, 0, (size_t)(chunks + 1) * 4, st)) != cudaSuccess) {
+            return e;
+        }
+        if (lookback) {
+            if (ct == 1u)
+                scan_lookback_list_kernel<1><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
+                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
+            else if (ct == 2u)
+                scan_lookback_list_kernel<2><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
+                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
+            else
+                scan_lookback_list_kernel<4><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
+                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
+        } else {
+            scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
+            scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
+            scan_apply_list_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec, g.cursor,
+                                                                   g.total + 1);
+        }
+        if (n) {
+            scatter_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, g.rank, n, g.meta, g.order);
+            cell_gather_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 4), kOrderWarps * 32, 0, st>>>(
+                g.meta, g.cursor, g.total + 1, g.order, g.photons, g.sorted, g.sorted_pos, wide);
         }
         return cudaGetLastError();
     }

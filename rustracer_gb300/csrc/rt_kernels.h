@@ -115,8 +115,9 @@ struct GridBuffers {
     uint32_t *scan_partials;  // grid_scan_partials(num_cells) entries
     uint32_t *total;          // 4 entries: [0] binned photons, [1] listed cells
     // Optional per-slot rank within its cell (null: count and an atomic scatter, then a pass that
-    // lists the multi-photon cells).  With ranks the count pass records them, the scatter needs no
-    // atomics and the scan lists the occupied cells.
+    // lists the multi-photon cells, a per-cell order pass and the gather).  With ranks the count pass
+    // records them, the scan lists the occupied cells, the scatter needs no atomics and one pass per
+    // occupied cell restores slot order and copies the records.
     uint32_t *rank;
 };
 uint32_t grid_scan_partials(uint32_t num_cells);
@@ -130,6 +131,8 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st);
 // launch with the value of the frame being replayed).
 // Denoise blocks whose TMA tile copies missed the wait bound since the library loaded (0 expected).
 uint32_t tma_timeouts();
+// Photon-grid scan chunks whose look-back gave up at the wait bound since the library loaded (0 expected).
+uint32_t scan_timeouts();
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
                            const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st);
 // accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass; alpha_dev as above.

@@ -415,6 +415,7 @@ extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_confi
 extern "C" uint64_t rt_renderer_device_bytes(const rt_renderer *r) { return r ? r->device_bytes() : 0; }
 
 extern "C" uint32_t rt_tma_timeouts(void) { return rtd::tma_timeouts(); }
+extern "C" uint32_t rt_scan_timeouts(void) { return rtd::scan_timeouts(); }
 
 extern "C" int rt_renderer_footprint(const rt_render_config *cfg, const rt_resident_scene *res, uint64_t *create_bytes,
                                      uint64_t *solo_path_bytes) {

@@ -197,6 +197,7 @@ def test_config3_photon_grid_full_size(gpu, orc):
     assert np.array_equal(meta, o.grid_meta)
     assert np.array_equal(srt[:o.binned].view(np.uint8), o.sorted[:o.binned].view(np.uint8))
     assert r.stats().photons_stored == o.binned > 1_000_000
+    assert rt._abi.load().rt_scan_timeouts() == 0
     o2 = oracle_for(orc, s, cfg, s.default_camera())
     o2.rebuild_photons()
     assert match_frac(ph.view(np.float32), o2.photons.view(np.float32), rtol=1e-4, atol=1e-4) >= 0.995

@@ -170,6 +170,13 @@ def random_photons(rng, n, gp, frac_invalid=0.2):
     ph["position"][:7] = np.array([np.nan, 0, 0], np.float32)  # NaN -> key 0 per axis
     # clustered photons: many share a cell (exercises the per-cell slot ordering beyond 32 and 1024)
     ph["position"][100:2600] = lo + span * np.float32(0.5)
+    # cells of about 40, 100, 200 and 300 photons at slots spread over the buffer (each cell-size class
+    # of the per-cell sort: one, two, four and eight entries per lane, and past the register sort)
+    rest = rng.permutation(np.arange(3000, n))
+    at = 0
+    for size, frac in ((50, 0.21), (125, 0.33), (250, 0.71), (375, 0.83)):
+        ph["position"][rest[at:at + size]] = lo + span * np.float32(frac)
+        at += size
     return ph
 
 
@@ -185,6 +192,8 @@ def test_photon_grid_stage_bit_exact(gpu, orc, grid_max_dim):
     assert np.array_equal(counts, c_o)
     assert np.array_equal(meta, m_o)
     assert np.array_equal(srt[:n].view(np.uint8), s_o[:n].view(np.uint8))
+    # every scan tile found its predecessors' sums within the look-back's wait bound
+    assert A.load().rt_scan_timeouts() == 0
 
 
 def test_photon_map_and_denoise_cornell(gpu, orc):
