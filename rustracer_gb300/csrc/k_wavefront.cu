@@ -335,9 +335,36 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
 // lookup and the debug views in; the host picks the variant that covers every job of the launch
 // (a job without photons or debug view takes the same path through either variant), so frames
 // without them run a smaller kernel.
+//
+// Each round a block takes 128 queue entries and orders them by what the hit needs -- a miss, a
+// dielectric, a Lambertian or emissive surface, a metal -- before shading, so a warp runs mostly one
+// of the loop body's branches (neighbouring paths hit triangles of unrelated materials).  Only the
+// order in which paths are shaded changes: each path's operations are its own, so images are the
+// same bit for bit.  Surviving paths, their shadow rays and photon-lookup requests are queued in the
+// paths' original order (which keeps neighbouring pixels together for the traversal).
 // ------------------------------------------------------------------------------------------------
+constexpr uint32_t kShadeKeys = 5;  // miss, dielectric, Lambertian / emissive, metal, no entry
+
+__device__ __forceinline__ uint32_t shade_key(const WaveParams &p, const uint32_t *q, uint32_t i, uint32_t n,
+                                              uint32_t &slot) {
+    slot = 0u;
+    if (i >= n) return 4u;
+    slot = q[i];
+    const float2 h = p.hit[slot];
+    if (h.x >= kInf) return 0u;
+    const DevScene &s = p.jobs[__float_as_uint(p.thr[slot].w)].scene;
+    const uint32_t mid = __float_as_uint(__ldg(s.tris + 8ull * clampi_u(__float_as_uint(h.y), s.tri_count) + 7).z);
+    const uint32_t kind = __float_as_uint(__ldg(s.mats + 4ull * clampi_u(mid, s.mat_count) + 2).z);
+    return kind == 2u ? 1u : (kind == 1u ? 3u : 2u);
+}
+
 template <bool kPhotons, bool kDebug>
 __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+    __shared__ uint32_t s_count[4][kShadeKeys];  // entries per warp and key
+    __shared__ uint32_t s_order[128];
+    __shared__ uint8_t s_emit[128];   // by original position: 1 survives, 2 shadow ray, 4 photon lookup
+    __shared__ uint32_t s_spos[128];  // by original position: shadow record index
+    __shared__ uint32_t s_ppos[128];  // by original position: photon-lookup record index
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
     uint32_t *q_next = p.queue[(iter + 1u) & 1u];
@@ -346,9 +373,31 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
     uint32_t *n_photon = p.counts + 4 * iter + 3u;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounds = (n + stride - 1u) / stride;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 
     for (uint32_t r = 0; r < rounds; ++r) {
-        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        // The block's entries ranked by key, stable (warp-major, then lane order within a key).
+        const uint32_t round_base = r * stride + blockIdx.x * blockDim.x;
+        const uint32_t i_own = round_base + threadIdx.x;
+        uint32_t slot_own;
+        const uint32_t key = shade_key(p, q, i_own, n, slot_own);
+        uint32_t same = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kShadeKeys; ++k) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
+            if (lane == k) s_count[warp][k] = __popc(m);
+            if (key == k) same = __popc(m & lanemask_lt());
+        }
+        __syncthreads();
+        uint32_t pos = same;
+#pragma unroll
+        for (uint32_t k = 0; k < kShadeKeys; ++k)
+#pragma unroll
+            for (uint32_t w = 0; w < 4; ++w)
+                if (k < key || (k == key && w < warp)) pos += s_count[w][k];
+        s_order[pos] = i_own;
+        __syncthreads();
+        const uint32_t i = s_order[threadIdx.x];
         const bool valid = i < n;
         bool keep = false;
         bool emit_shadow = false, emit_photon = false;
@@ -587,39 +636,48 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
             if (sidx0 < 8u) reinterpret_cast<float *>(acc + 2)[sidx0] = A.sl;
             if (first_hit) p.nrm[slot] = nrm;
         }
-        // NEE shadow ray (deferred) and the continuing path.
+        // Queue positions by original order: each thread appends for the entry it keyed, then the
+        // thread that shaded it writes its records there.
+        const uint32_t li = i - round_base;
+        s_emit[li] = (keep ? 1u : 0u) | (emit_shadow ? 2u : 0u) | ((kPhotons && emit_photon) ? 4u : 0u);
+        __syncthreads();
         {
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, emit_shadow);
-            if (mask) {
-                const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
+            const uint32_t e = s_emit[threadIdx.x];
+            warp_append((e & 1u) != 0u, slot_own, q_next, n_next);
+            const uint32_t ms = __ballot_sync(0xFFFFFFFFu, (e & 2u) != 0u);
+            if (ms) {
+                const uint32_t leader = __ffs(ms) - 1u;
                 uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(n_shadow, (uint32_t)__popc(mask));
+                if (lane == leader) base = atomicAdd(n_shadow, (uint32_t)__popc(ms));
                 base = __shfl_sync(0xFFFFFFFFu, base, leader);
-                if (emit_shadow) {
-                    float4 *rec = p.shadow + 3ull * (base + __popc(mask & lanemask_lt()));
-                    rec[0] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_max);
-                    rec[1] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(slot));
-                    rec[2] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sh_tag));
+                if (e & 2u) s_spos[threadIdx.x] = base + __popc(ms & lanemask_lt());
+            }
+            if (kPhotons) {
+                const uint32_t mp = __ballot_sync(0xFFFFFFFFu, (e & 4u) != 0u);
+                if (mp) {
+                    const uint32_t leader = __ffs(mp) - 1u;
+                    uint32_t base = 0;
+                    if (lane == leader) base = atomicAdd(n_photon, (uint32_t)__popc(mp));
+                    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                    if (e & 4u) s_ppos[threadIdx.x] = base + __popc(mp & lanemask_lt());
                 }
             }
         }
-        if (kPhotons) {
-            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, emit_photon);
-            if (mask) {
-                const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1u;
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(n_photon, (uint32_t)__popc(mask));
-                base = __shfl_sync(0xFFFFFFFFu, base, leader);
-                if (emit_photon) {
-                    float4 *rec = p.preq + 3ull * (base + __popc(mask & lanemask_lt()));
-                    const uint32_t jid = __float_as_uint(p.thr[slot].w);
-                    rec[0] = make_float4(ph_hp.x, ph_hp.y, ph_hp.z, __uint_as_float(slot));
-                    rec[1] = make_float4(ph_n.x, ph_n.y, ph_n.z, __uint_as_float(ph_sidx));
-                    rec[2] = make_float4(ph_td.x, ph_td.y, ph_td.z, __uint_as_float(jid));
-                }
-            }
+        __syncthreads();
+        // NEE shadow ray (deferred) and the photon-map lookup request.
+        if (emit_shadow) {
+            float4 *rec = p.shadow + 3ull * s_spos[li];
+            rec[0] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_max);
+            rec[1] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(slot));
+            rec[2] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sh_tag));
         }
-        warp_append(keep, slot, q_next, n_next);
+        if (kPhotons && emit_photon) {
+            float4 *rec = p.preq + 3ull * s_ppos[li];
+            const uint32_t jid = __float_as_uint(p.thr[slot].w);
+            rec[0] = make_float4(ph_hp.x, ph_hp.y, ph_hp.z, __uint_as_float(slot));
+            rec[1] = make_float4(ph_n.x, ph_n.y, ph_n.z, __uint_as_float(ph_sidx));
+            rec[2] = make_float4(ph_td.x, ph_td.y, ph_td.z, __uint_as_float(jid));
+        }
     }
 }
 
