@@ -370,7 +370,7 @@ typedef struct rt_batch rt_batch;
  * 256, blocks_per_sm up to 2048 / block_threads, chunk (queue items a warp takes per atomic, its
  * segment of the shared queue) 32 .. 1024 in steps of 32, steps (traversal records between lane
  * refills) 1 .. 64, stack_entries 32 / 48 / 64 per lane, raised to what the jobs' trees need.
- * Default: 128 threads, 8 blocks per SM, chunk 64, 8 steps, 32 entries. */
+ * Default: 128 threads, 8 blocks per SM, chunk 32, 4 steps, 32 entries. */
 typedef struct rt_wavefront_tuning {
     uint32_t block_threads, blocks_per_sm, chunk, steps, stack_entries;
     uint32_t _pad[3];

@@ -917,7 +917,7 @@ __global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t i
 // ------------------------------------------------------------------------------------------------
 // Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
-WaveTuning default_tuning() { return WaveTuning{128u, 8u, 64u, 8u, 32u}; }
+WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u}; }
 
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     const WaveTuning in = t;
