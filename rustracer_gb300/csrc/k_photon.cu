@@ -749,13 +749,23 @@ __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__rest
 }
 
 // ---- grid build with per-slot ranks ---------------------------------------------------------------
+// The kernels after the count are launched as programmatic dependents of the one before: their blocks
+// may be scheduled while it finishes, and wait here until it has completed and its writes are visible.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel's blocks be scheduled as this grid's blocks retire (they wait for completion).
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // Histogram with ranks: counts[key] += 1 and rank[slot] = the count found before the add (the slot's
 // position within its cell, in atomic order).
 __global__ void __launch_bounds__(256) count_rank_kernel(const uint32_t *__restrict__ keys, uint64_t n,
                                                          uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
-                                                         uint32_t *__restrict__ clear, uint32_t n_clear) {
-    // the scan's chunk status words and ticket start at zero (this launch precedes the scan)
+                                                         uint32_t *__restrict__ clear, uint32_t n_clear,
+                                                         uint32_t *__restrict__ n_list) {
+    grid_launch_dependents();
+    // the scan's chunk status words and ticket, and its count of listed cells, start at zero (this
+    // launch precedes the scan)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_clear; i += gridDim.x * blockDim.x) clear[i] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_list = 0u;
     // eight keys per thread and pass (two 16-byte loads in flight), then the adds, then the ranks
     const uint64_t stride = 8ull * gridDim.x * blockDim.x;
     const uint64_t start = 4ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
@@ -847,21 +857,21 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_list_kernel(const uin
 constexpr uint32_t kScanFlagAgg = 1u << 30, kScanFlagIncl = 2u << 30, kScanValMask = (1u << 30) - 1u;
 __device__ unsigned int g_scan_timeouts = 0u;
 
-__device__ __forceinline__ void load_counts8(const uint32_t *__restrict__ counts, uint32_t base, uint32_t n, bool vec,
+__device__ __forceinline__ void load_counts8(const uint32_t *counts, uint32_t base, uint32_t n, bool vec,
                                              uint32_t (&v)[kScanItems]) {
     if (vec && base + kScanItems <= n) {
-        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(counts + base));
-        const uint4 b = __ldg(reinterpret_cast<const uint4 *>(counts + base + 4));
+        const uint4 a = *reinterpret_cast<const uint4 *>(counts + base);
+        const uint4 b = *reinterpret_cast<const uint4 *>(counts + base + 4);
         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
         v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
     } else {
 #pragma unroll
-        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? __ldg(counts + base + i) : 0u;
+        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? counts[base + i] : 0u;
     }
 }
 
 template <int CT>
-__global__ void __launch_bounds__(kScanThreads) scan_lookback_list_kernel(const uint32_t *__restrict__ counts,
+__global__ void __launch_bounds__(kScanThreads) scan_lookback_list_kernel(uint32_t *__restrict__ counts,
                                                                           uint32_t n, uint32_t *status,
                                                                           uint32_t chunks, uint2 *__restrict__ meta,
                                                                           bool vec, uint32_t *__restrict__ list,
@@ -869,6 +879,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_lookback_list_kernel(const 
                                                                           uint32_t *__restrict__ total_out) {
     __shared__ uint32_t warp_sums[kScanThreads / 32];
     __shared__ uint32_t s_chunk, s_prefix;
+    grid_dependency_wait();
+    grid_launch_dependents();
     if (threadIdx.x == 0) s_chunk = atomicAdd(status + chunks, 1u);
     __syncthreads();
     const uint32_t chunk = s_chunk;
@@ -945,15 +957,21 @@ __global__ void __launch_bounds__(kScanThreads) scan_lookback_list_kernel(const 
             st[i] = ex;
             ex += v[t][i];
         }
+        // (start, count) written; the counts are cleared for the next build (meta keeps them)
         if (vec && base + kScanItems <= n) {
             uint4 *m4 = reinterpret_cast<uint4 *>(meta + base);
 #pragma unroll
             for (uint32_t i = 0; i < kScanItems; i += 2)
                 m4[i / 2] = make_uint4(st[i], v[t][i], st[i + 1], v[t][i + 1]);
+            reinterpret_cast<uint4 *>(counts + base)[0] = make_uint4(0u, 0u, 0u, 0u);
+            reinterpret_cast<uint4 *>(counts + base)[1] = make_uint4(0u, 0u, 0u, 0u);
         } else {
 #pragma unroll
             for (uint32_t i = 0; i < kScanItems; ++i)
-                if (base + i < n) meta[base + i] = make_uint2(st[i], v[t][i]);
+                if (base + i < n) {
+                    meta[base + i] = make_uint2(st[i], v[t][i]);
+                    counts[base + i] = 0u;
+                }
         }
         // warp-exclusive offsets of the occupied cells, one atomic per warp
         uint32_t x = occ;
@@ -984,6 +1002,8 @@ __global__ void __launch_bounds__(256) scatter_rank_kernel(const uint32_t *__res
                                                            const uint32_t *__restrict__ rank, uint64_t n,
                                                            const uint2 *__restrict__ meta,
                                                            uint32_t *__restrict__ order) {
+    grid_dependency_wait();
+    grid_launch_dependents();
     // eight keys per thread and pass (two 16-byte loads in flight), then the starts and ranks, then the
     // stores
     const uint64_t stride = 8ull * gridDim.x * blockDim.x;
@@ -1083,6 +1103,7 @@ __global__ void __launch_bounds__(kOrderWarps * 32, 4) cell_gather_kernel(const 
                                                                        float4 *__restrict__ sorted,
                                                                        float4 *__restrict__ sorted_pos, bool wide) {
     __shared__ uint32_t sbuf[kOrderWarps][kCellRegsMax];
+    grid_dependency_wait();
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     uint32_t *buf = sbuf[w];
     const uint32_t warps_total = gridDim.x * kOrderWarps;
@@ -1110,6 +1131,24 @@ __global__ void __launch_bounds__(kOrderWarps * 32, 4) cell_gather_kernel(const 
     }
 }
 
+// Launches `kernel` as a programmatic dependent of the previous kernel in the stream: its blocks may
+// be scheduled before that kernel has finished and wait for it in grid_dependency_wait().
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t st,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
     cudaError_t e;
     const uint32_t C = g.num_cells;
@@ -1125,46 +1164,52 @@ cudaError_t launch_grid_build(const GridBuffers &g, cudaStream_t st) {
     const bool wide = ((reinterpret_cast<uintptr_t>(g.photons) | reinterpret_cast<uintptr_t>(g.sorted)) % 32u) == 0u;
     const uint32_t tiles = (C + kScanTile - 1) / kScanTile;
     if (g.rank) {
-        if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
-        // The occupied cells are listed in the cursor array (no cursors are needed with ranks); the
-        // list length is total[1].
-        if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
         // One scan pass with decoupled look-back while every value fits its 30 bits, else the three
         // phases.  Chunks of up to four tiles, about two chunks per SM; the look-back's chunk status
-        // words and ticket (scan_partials[0 .. chunks], chunks <= tiles) are cleared by the count
-        // launch (or by a memset when there are no slots to count).
-        const bool lookback = n < (uint64_t)kScanValMask;
+        // words and ticket (scan_partials[0 .. chunks], chunks <= tiles) and the count of occupied cells
+        // (total[1]; the cells are listed in the cursor array, which this path does not otherwise need)
+        // are cleared by the count launch.  The counts are zero on entry: cleared when the renderer is
+        // created and by the scan of every build once it has turned them into (start, count).
+        const bool lookback = n && n < (uint64_t)kScanValMask;
         const uint32_t want = (tiles + 2 * sm - 1) / (2 * sm);
         const uint32_t ct = want <= 1u ? 1u : (want <= 2u ? 2u : 4u);
         const uint32_t chunks = (tiles + ct - 1) / ct;
-        if (n) {
-            count_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank,
-                                                                             g.scan_partials, lookback ? chunks + 1 : 0u);
-        } else if ((e = cudaMemsetAsync(g.scan_partials, 0, (size_t)(chunks + 1) * 4, st)) != cudaSuccess) {
-            return e;
-        }
-        if (lookback) {
-            if (ct == 1u)
-                scan_lookback_list_kernel<1><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
-                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
-            else if (ct == 2u)
-                scan_lookback_list_kernel<2><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
-                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
-            else
-                scan_lookback_list_kernel<4><<<chunks, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, chunks,
-                                                                              g.meta, vec, g.cursor, g.total + 1, g.total);
-        } else {
+        if (!lookback) {
+            if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(g.total + 1, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+            if (n) count_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank, nullptr,
+                                                                                    0u, g.total + 1);
             scan_reduce_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials);
             scan_partials_kernel<<<1, kScanThreads, 0, st>>>(g.scan_partials, tiles, g.total);
             scan_apply_list_kernel<<<tiles, kScanThreads, 0, st>>>(g.counts, C, g.scan_partials, g.meta, vec, g.cursor,
                                                                    g.total + 1);
+            if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
+            if (n) {
+                scatter_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, g.rank, n, g.meta, g.order);
+                cell_gather_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 4), kOrderWarps * 32, 0, st>>>(
+                    g.meta, g.cursor, g.total + 1, g.order, g.photons, g.sorted, g.sorted_pos, wide);
+            }
+            return cudaGetLastError();
         }
-        if (n) {
-            scatter_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, g.rank, n, g.meta, g.order);
-            cell_gather_kernel<<<grid_for((uint64_t)C * 32, kOrderWarps * 32, 4), kOrderWarps * 32, 0, st>>>(
-                g.meta, g.cursor, g.total + 1, g.order, g.photons, g.sorted, g.sorted_pos, wide);
-        }
-        return cudaGetLastError();
+        count_rank_kernel<<<grid_for((n + 7) / 8, 256, 8), 256, 0, st>>>(g.keys, n, g.counts, g.rank, g.scan_partials,
+                                                                         chunks + 1, g.total + 1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (ct == 1u)
+            e = launch_dependent(scan_lookback_list_kernel<1>, chunks, kScanThreads, st, g.counts, C, g.scan_partials,
+                                 chunks, g.meta, vec, g.cursor, g.total + 1, g.total);
+        else if (ct == 2u)
+            e = launch_dependent(scan_lookback_list_kernel<2>, chunks, kScanThreads, st, g.counts, C, g.scan_partials,
+                                 chunks, g.meta, vec, g.cursor, g.total + 1, g.total);
+        else
+            e = launch_dependent(scan_lookback_list_kernel<4>, chunks, kScanThreads, st, g.counts, C, g.scan_partials,
+                                 chunks, g.meta, vec, g.cursor, g.total + 1, g.total);
+        if (e != cudaSuccess) return e;
+        if ((e = launch_dependent(scatter_rank_kernel, grid_for((n + 7) / 8, 256, 8), 256, st, g.keys,
+                                  (const uint32_t *)g.rank, n, (const uint2 *)g.meta, g.order)) != cudaSuccess)
+            return e;
+        return launch_dependent(cell_gather_kernel, grid_for((uint64_t)C * 32, kOrderWarps * 32, 4), kOrderWarps * 32, st,
+                                (const uint2 *)g.meta, (const uint32_t *)g.cursor, (const uint32_t *)(g.total + 1),
+                                g.order, g.photons, g.sorted, g.sorted_pos, wide);
     }
     if ((e = cudaMemsetAsync(g.counts, 0, (size_t)C * 4, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(g.cursor, 0, (size_t)C * 4, st)) != cudaSuccess) return e;

@@ -884,14 +884,20 @@ extern "C" int rt_read_photon_grid(rt_renderer *r, uint32_t *counts, uint32_t *m
                   r->gp.num_cells);
         return RT_ERR_INVALID_ARGUMENT;
     }
-    if (counts) {
-        if (int st = read_back(r, r->d_counts, counts, num_cells * 4, (uint64_t)r->gp.num_cells * 4, "rt_read_photon_grid"))
-            return st;
+    // The build turns the per-cell counts into (start, count) pairs and clears them for the next
+    // build, so the counts are read from the pairs.
+    const uint64_t C = r->gp.num_cells;
+    std::vector<uint32_t> pairs;
+    uint32_t *m = meta;
+    if (!m && counts) {
+        pairs.resize(2 * C);
+        m = pairs.data();
     }
-    if (meta) {
-        if (int st = read_back(r, r->d_meta, meta, num_cells * 8, (uint64_t)r->gp.num_cells * 8, "rt_read_photon_grid"))
-            return st;
+    if (m) {
+        if (int st = read_back(r, r->d_meta, m, (meta ? num_cells : C) * 8, C * 8, "rt_read_photon_grid")) return st;
     }
+    if (counts)
+        for (uint64_t c = 0; c < C; ++c) counts[c] = m[2 * c + 1];
     return RT_OK;
 }
 
@@ -983,6 +989,7 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     if (S) RT_CK(cudaMemcpy(ph.p, photons, S * 64, cudaMemcpyHostToDevice));
     RT_CK(cudaMemset(srt.p, 0, S * 64 ? S * 64 : 16));
     RT_CK(cudaMemset(tot.p, 0, 16));
+    RT_CK(cudaMemset(cnt.p, 0, C * 4));  // the build expects zero counts and leaves them zero
     RT_CK(rtd::launch_photon_keys(ph.as<float4>(), S, gp, keys.as<uint32_t>(), 0));
     rtd::GridBuffers g;
     g.photons = ph.as<float4>();
@@ -999,8 +1006,8 @@ extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_para
     g.total = tot.as<uint32_t>();
     g.rank = rank.as<uint32_t>();
     RT_CK(rtd::launch_grid_build(g, 0));
-    RT_CK(cudaMemcpy(counts, cnt.p, C * 4, cudaMemcpyDeviceToHost));
     RT_CK(cudaMemcpy(meta, mt.p, C * 8, cudaMemcpyDeviceToHost));
+    for (uint64_t c = 0; c < C; ++c) counts[c] = meta[2 * c + 1];  // the build cleared the counts
     if (S) RT_CK(cudaMemcpy(sorted, srt.p, S * 64, cudaMemcpyDeviceToHost));
     return RT_OK;
 }
