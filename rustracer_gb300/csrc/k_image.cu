@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
     constexpr int H = 2 * kStep, TW = kDnBX + 2 * H, TH = kDnRows + 2 * H;
     constexpr uint32_t kBox = 16u * TW * TH;  // bytes of one staged tile
     extern __shared__ unsigned char dn_raw[];
+    grid_launch_dependents();
     // TMA writes the tiles at a 128-byte aligned shared address; the mbarrier follows the tiles.
     float4 *dn_smem = reinterpret_cast<float4 *>(
         (reinterpret_cast<uintptr_t>(dn_raw) + 127u) & ~static_cast<uintptr_t>(127u));
@@ -228,18 +229,22 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    // A pass after another pass may start while that one finishes (programmatic dependent launch):
+    // the G-buffer tile and the moments are the frame's, only the colour tile is the previous pass's
+    // output, so its copy is issued after grid_dependency_wait().
     if (tid == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s), "r"(2u * kBox) : "memory");
         const int cx = x0 - H, cy = y0t - H;
         asm volatile(
             "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
-                (uint32_t)__cvta_generic_to_shared(&s_cl[0][0])),
-            "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
                 (uint32_t)__cvta_generic_to_shared(&s_nd[0][0])),
             "l"(reinterpret_cast<uint64_t>(&tm_g)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
+            : "memory");
+        grid_dependency_wait();
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(&s_cl[0][0])),
+            "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(0), "r"(cx), "r"(cy), "r"(bar_s)
             : "memory");
     }
     // Variance window ((32 + 2) x (32 + 2), -1 outside the image): columns 0..31 at rows
@@ -265,6 +270,7 @@ __global__ void __launch_bounds__(kDnBX * kDnThreadsY, 3) denoise_tiled_kernel(c
         }
         if (tid < 2 * VH) s_var[ey][ex] = inside(egx, egy) ? fmaxf(me.y - me.x * me.x, 0.0f) : -1.0f;
     }
+    grid_dependency_wait();  // nothing below reads or writes what the previous pass uses before it ends
     // Wait for the two tiles (phase 0 of the barrier), bounded: a block whose copies do not arrive
     // counts the fault, waits once more (bounded) for them and leaves without writing.
     if (__syncthreads_or(!mbar_wait(bar_s, 0u)) != 0) {
@@ -385,7 +391,7 @@ uint32_t tma_timeouts() {
 }
 
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
-                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st) {
+                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st, bool after_pass) {
     if (p.step_size == 1u || p.step_size == 2u) {
         prepare_kernels();
         dim3 block(kDnBX, kDnThreadsY);
@@ -395,11 +401,20 @@ cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer,
         cudaError_t e;
         if ((e = encode_tile_map(&tm_in, in, p.width, p.height, side)) != cudaSuccess) return e;
         if ((e = encode_tile_map(&tm_g, gbuffer, p.width, p.height, side)) != cudaSuccess) return e;
+        // A pass right after another tiled pass is a programmatic dependent of it.
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = p.step_size == 1u ? denoise_smem_bytes<1>() : denoise_smem_bytes<2>();
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = after_pass ? 1 : 0;
         if (p.step_size == 1u)
-            denoise_tiled_kernel<1><<<grid, block, denoise_smem_bytes<1>(), st>>>(tm_in, tm_g, out, moments, p, alpha_dev);
-        else
-            denoise_tiled_kernel<2><<<grid, block, denoise_smem_bytes<2>(), st>>>(tm_in, tm_g, out, moments, p, alpha_dev);
-        return cudaGetLastError();
+            return cudaLaunchKernelEx(&cfg, denoise_tiled_kernel<1>, tm_in, tm_g, out, moments, p, alpha_dev);
+        return cudaLaunchKernelEx(&cfg, denoise_tiled_kernel<2>, tm_in, tm_g, out, moments, p, alpha_dev);
     }
     dim3 block(32, 8);
     dim3 grid((p.width + block.x - 1) / block.x, (p.height + block.y - 1) / block.y);

@@ -749,11 +749,8 @@ __global__ void __launch_bounds__(256) photon_gather_kernel(const float4 *__rest
 }
 
 // ---- grid build with per-slot ranks ---------------------------------------------------------------
-// The kernels after the count are launched as programmatic dependents of the one before: their blocks
-// may be scheduled while it finishes, and wait here until it has completed and its writes are visible.
-__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-// Lets the next kernel's blocks be scheduled as this grid's blocks retire (they wait for completion).
-__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+// The kernels after the count are launched as programmatic dependents of the one before (their blocks
+// may be scheduled while it finishes and wait for it in grid_dependency_wait).
 
 // Histogram with ranks: counts[key] += 1 and rank[slot] = the count found before the add (the slot's
 // position within its cell, in atomic order).

@@ -590,6 +590,14 @@ __device__ __forceinline__ void tangent_frame(const TriFull &tri, f3 n, f3 &t_ou
 }
 __device__ __forceinline__ f3 triangle_normal(f3 v0, f3 v1, f3 v2) { return normalize(cross(v1 - v0, v2 - v0)); }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic-serialization attribute may
+// start while the kernel before it in the stream finishes; grid_dependency_wait() returns once that
+// kernel has completed and its writes are visible (at once for a kernel launched the ordinary way).
+// grid_launch_dependents() lets the next such kernel's blocks be scheduled as this grid's blocks
+// retire.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // Warp helpers of the queue kernels.
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

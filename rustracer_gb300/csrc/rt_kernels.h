@@ -134,7 +134,7 @@ uint32_t tma_timeouts();
 // Photon-grid scan chunks whose look-back gave up at the wait bound since the library loaded (0 expected).
 uint32_t scan_timeouts();
 cudaError_t launch_denoise(const float4 *in, float4 *out, const float4 *gbuffer, const float4 *moments,
-                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st);
+                           const rt_denoise_params &p, const float *alpha_dev, cudaStream_t st, bool after_pass = false);
 // accum = mix(accum, frame, alpha) and the tonemapped rgba8 image in one pass; alpha_dev as above.
 cudaError_t launch_resolve(const float4 *frame, float4 *accum, const float4 *gbuffer, uint32_t width,
                            uint32_t height, float alpha, const float *alpha_dev, const rt_tonemap_params &tp,

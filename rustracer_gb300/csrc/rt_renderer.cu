@@ -495,7 +495,8 @@ int enqueue_denoise(rt_renderer *r, float alpha, const float *alpha_dev, cudaStr
         dp.alpha = alpha;
         const float4 *in = (it % 2 == 0) ? r->d_frame.as<float4>() : r->d_pingpong.as<float4>();
         float4 *o = (it % 2 == 0) ? r->d_pingpong.as<float4>() : r->d_frame.as<float4>();
-        RT_CK(rtd::launch_denoise(in, o, r->d_gbuffer.as<float4>(), r->d_moments.as<float4>(), dp, alpha_dev, s));
+        RT_CK(rtd::launch_denoise(in, o, r->d_gbuffer.as<float4>(), r->d_moments.as<float4>(), dp, alpha_dev, s,
+                                  it == 1u));
         result = o;
     }
     r->last_denoise_passes = passes;
