@@ -180,7 +180,9 @@ def random_photons(rng, n, gp, frac_invalid=0.2):
     return ph
 
 
-@pytest.mark.parametrize("grid_max_dim", [26, 130])
+# 26: the reference's grid (one scan tile per look-back chunk); 102: 100^3 cells (two tiles per chunk
+# on a 152-SM GPU); 130: 128^3 cells (four tiles per chunk)
+@pytest.mark.parametrize("grid_max_dim", [26, 102, 130])
 def test_photon_grid_stage_bit_exact(gpu, orc, grid_max_dim):
     gp, _ = rt.derive_grid((np.zeros(3), np.full(3, 555.0)), grid_max_dim, 1 if grid_max_dim > 26 else 0, 1)
     rng = np.random.default_rng(grid_max_dim)
