@@ -349,7 +349,8 @@ int rt_read_gbuffer(rt_renderer *r, float *rgba, uint64_t n_floats);       /* W*
 int rt_read_tonemapped(rt_renderer *r, uint8_t *rgba8, uint64_t n_bytes);  /* W*H*4 */
 int rt_read_photons(rt_renderer *r, rt_photon *out, uint64_t n);           /* photon_slots */
 int rt_read_sorted_photons(rt_renderer *r, rt_photon *out, uint64_t n);    /* photon_slots */
-/* counts: num_cells u32; meta: num_cells (start, count) pairs. */
+/* counts: num_cells u32; meta: num_cells (start, count) pairs (either may be null).  The counts are
+ * the pairs' second members (the device count buffer is cleared by the build once scanned). */
 int rt_read_photon_grid(rt_renderer *r, uint32_t *counts, uint32_t *meta, uint64_t num_cells);
 /* Replaces the traced photon slots (n == photon_slots) and rebuilds the grid from them, skipping the
  * trace: lets a caller feed an identical photon buffer to this backend and to another one. */
