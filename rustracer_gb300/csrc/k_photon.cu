@@ -679,14 +679,16 @@ struct Photon8 {
     float v[16];
 };
 
-// 64 bytes as two 32-byte accesses (the records are 64-byte aligned when `wide`).
+// 64 bytes as two 32-byte accesses (the records are 64-byte aligned when `wide`).  The L2 fetch size
+// is held to 64 bytes: a record's neighbour in its 128-byte line belongs to another cell, and fetching
+// whole lines made the per-cell copy read 1.7x the photon bytes it needs from DRAM.
 __device__ __forceinline__ void load_photon_wide(const float4 *src, Photon8 &p) {
     const float *f = reinterpret_cast<const float *>(src);
-    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm volatile("ld.global.nc.L2::64B.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(p.v[0]), "=f"(p.v[1]), "=f"(p.v[2]), "=f"(p.v[3]), "=f"(p.v[4]), "=f"(p.v[5]), "=f"(p.v[6]),
                    "=f"(p.v[7])
                  : "l"(f));
-    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm volatile("ld.global.nc.L2::64B.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(p.v[8]), "=f"(p.v[9]), "=f"(p.v[10]), "=f"(p.v[11]), "=f"(p.v[12]), "=f"(p.v[13]),
                    "=f"(p.v[14]), "=f"(p.v[15])
                  : "l"(f + 8));
