@@ -5,7 +5,8 @@
 //                         bounce body also emits the u32 cell key of every slot it stores
 //                         (photon_count.wgsl:18-23), so the grid build never re-reads positions.
 //   photon_keys_kernel    keys of a photon buffer loaded from the host (same key function).
-//   grid build            exact u32 counting sort of the slots by cell key:
+//   grid build            exact u32 counting sort of the slots by cell key; without per-slot ranks
+//                         (the no-allocation entry, whose scratch holds no rank array):
 //     count_kernel        histogram (photon_count.wgsl:25-34)
 //     scan_*              device exclusive scan of the counts into (start, count) pairs; replaces the
 //                         blocking read-back and host scan of lib.rs:956-1007
@@ -15,10 +16,10 @@
 //                         slot order, independent of atomic arrival order (the reference's order
 //                         within a cell is unspecified)
 //     gather_kernel       sorted[i] = photons[order[i]] (64-byte records)
-//   grid build with ranks (the renderer's path): count_rank (histogram + each slot's rank in atomic
-//   order), scan_lookback_list (single-pass scan + list of occupied cells), scatter_rank (start + rank,
-//   no atomics), then cell_gather: per occupied cell the slot order restored and the records copied
-//   in one pass.
+//   grid build with ranks (the renderer's and the stage entry's path): count_rank (histogram + each
+//   slot's rank in atomic order), scan_lookback_list (single-pass scan + list of occupied cells),
+//   scatter_rank (start + rank, no atomics), then cell_gather: per occupied cell the slot order
+//   restored and the records copied in one pass.  Same counts, offsets and slot order either way.
 #include <algorithm>
 #include <cstring>
 
