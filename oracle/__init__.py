@@ -66,6 +66,7 @@ PHOTON_DTYPE = np.dtype([("position", "<f4", 3), ("_pad0", "<f4"), ("power", "<f
 vp = C.c_void_p
 _PROTOS = {
     "oracle_rng_sequence": (u32, [u32, u32, vp, vp]),
+    "oracle_sincos": (None, [vp, C.c_uint64, vp, vp]),
     "oracle_intersect_triangle": (C.c_float, [vp, vp, vp, vp, vp]),
     "oracle_trace_rays": (None, [vp, vp, vp, C.c_uint64, vp, vp, C.c_int]),
     "oracle_gather": (C.c_int, [vp, C.POINTER(CameraUniform), C.POINTER(ImageParams), u32, C.POINTER(GridParams),
@@ -118,6 +119,15 @@ def rng_sequence(seed: int, n: int) -> tuple[np.ndarray, np.ndarray]:
     f = np.empty(n, np.float32)
     load().oracle_rng_sequence(seed, n, _p(u), _p(f))
     return u, f
+
+
+def sincos(x: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The fixed-sequence sin and cos both backends use for sampling angles."""
+    a = np.ascontiguousarray(x, np.float32)
+    s = np.empty_like(a)
+    c = np.empty_like(a)
+    load().oracle_sincos(_p(a), len(a), _p(s), _p(c))
+    return s, c
 
 
 def trace_rays(scene_desc, origins: np.ndarray, dirs: np.ndarray, threads: int = 0):
@@ -257,22 +267,30 @@ class OracleRenderer:
             return 1.0
         return float(np.float32(1.0) / np.float32(min(self.frames_since_reset, n)))
 
-    def record_frame(self, rows: tuple[int, int] | None = None) -> None:
-        """record_frame (lib.rs:666-851); rows restricts the gather to a row range (timing samples)."""
+    def record_frame(self, rows=None) -> None:
+        """record_frame (lib.rs:666-851).  rows restricts the gather to a row range (r0, r1) or to a list
+        of such ranges (sampled rows of a large frame); the other rows of frame, moments and gbuffer keep
+        their contents, and the denoise / composite / tonemap stages run over the whole image."""
         c = self.cfg
         self.sample_counter = (self.sample_counter + 1) & 0xFFFFFFFF
         self.frames_since_reset = min(self.frames_since_reset + 1, 0xFFFFFFFF)
         alpha = self.alpha()
         ip = self.image_params(alpha)
-        r0, r1 = rows if rows else (0, c.height)
+        if rows is None:
+            ranges = [(0, c.height)]
+        elif isinstance(rows[0], (tuple, list)):
+            ranges = [tuple(r) for r in rows]
+        else:
+            ranges = [tuple(rows)]
         mb = c.max_bounces or 6
         use = ip.use_photons == 1
-        st = load().oracle_gather(C.cast(C.pointer(self.desc), vp), C.byref(self.cam), C.byref(ip), mb,
-                                  C.byref(self.gp), _p(self.sorted) if use else None, len(self.sorted),
-                                  _p(self.grid_meta) if use else None, r0, r1, self.threads, _p(self.frame),
-                                  _p(self.moments), _p(self.gbuffer), _p(self.counters))
-        if st != 0:
-            raise RuntimeError("oracle_gather rejected its arguments")
+        for r0, r1 in ranges:
+            st = load().oracle_gather(C.cast(C.pointer(self.desc), vp), C.byref(self.cam), C.byref(ip), mb,
+                                      C.byref(self.gp), _p(self.sorted) if use else None, len(self.sorted),
+                                      _p(self.grid_meta) if use else None, r0, r1, self.threads, _p(self.frame),
+                                      _p(self.moments), _p(self.gbuffer), _p(self.counters))
+            if st != 0:
+                raise RuntimeError("oracle_gather rejected its arguments")
         result = self.frame
         if c.enable_denoise:
             result = denoise(self.frame, self.gbuffer, self.moments, alpha, c.denoise_passes or 2, self.threads)

@@ -79,6 +79,28 @@ inline int32_t f2i(float f) {  // WGSL i32(f32)
     return (int32_t)f;
 }
 
+// sin, cos and the integer powers pow(x, 2) / pow(x, 5).  WGSL leaves their accuracy to the backend
+// (sin and cos need only 2^-11 absolute error), so the restatement fixes one sequence of IEEE
+// operations for them, the one the CUDA backend uses: Cody-Waite reduction by pi/2 with the two-part
+// constant 1.5703125 + 4.83826794e-4 (Cody and Waite, Software Manual for the Elementary Functions,
+// 1980), then the Taylor series of sin through x^9 and of cos through x^10 on [-pi/4, pi/4], Horner
+// form; pow(x, 0.5) on [0, 1] is sqrt(x), pow(x, 2) is x * x, pow(x, 5) is (x^2)^2 * x.
+inline void sincos_fixed(float x, float &s, float &c) {
+    const float k = std::floor(x * 0.636619772f + 0.5f);
+    const float r = (x - k * 1.5703125f) - k * 4.83826794e-4f;
+    const float z = r * r;
+    const float sr = r + r * z * (-(1.0f / 6.0f) + z * ((1.0f / 120.0f) + z * (-(1.0f / 5040.0f) + z * (1.0f / 362880.0f))));
+    const float cr = 1.0f - 0.5f * z +
+                     z * z * ((1.0f / 24.0f) + z * (-(1.0f / 720.0f) + z * ((1.0f / 40320.0f) + z * -(1.0f / 3628800.0f))));
+    const int q = (int)k & 3;
+    s = q == 0 ? sr : (q == 1 ? cr : (q == 2 ? -sr : -cr));
+    c = q == 0 ? cr : (q == 1 ? -sr : (q == 2 ? -cr : sr));
+}
+inline float pow5(float x) {
+    const float x2 = x * x;
+    return x2 * x2 * x;
+}
+
 // ---- common.wgsl:12-25 ------------------------------------------------------------------------
 inline V3 reflect(V3 v, V3 n) { return v - 2.0f * dot(v, n) * n; }
 inline V3 refract(V3 v, V3 n, float eta) {
@@ -88,7 +110,7 @@ inline V3 refract(V3 v, V3 n, float eta) {
     return r_out_perp + r_out_parallel;
 }
 inline V3 fresnel_schlick(float cos_theta, V3 f0) {
-    float p = std::pow(clampf(1.0f - cos_theta, 0.0f, 1.0f), 5.0f);
+    float p = pow5(clampf(1.0f - cos_theta, 0.0f, 1.0f));
     return f0 + (mk(1.0f, 1.0f, 1.0f) - f0) * p;
 }
 
@@ -119,7 +141,9 @@ inline V3 sample_cosine_hemisphere(Rng &r) {
     float phi = 2.0f * PI * u1;
     float cos_theta = std::sqrt(u2);
     float sin_theta = std::sqrt(1.0f - u2);
-    return mk(std::cos(phi) * sin_theta, cos_theta, std::sin(phi) * sin_theta);
+    float sp, cp;
+    sincos_fixed(phi, sp, cp);
+    return mk(cp * sin_theta, cos_theta, sp * sin_theta);
 }
 inline V3 to_world(V3 local, V3 normal) {
     V3 up = std::fabs(normal.y) < 0.999f ? mk(0, 1, 0) : mk(1, 0, 0);
@@ -369,7 +393,7 @@ inline bool shadowed(const GatherCtx &g, V3 origin, V3 dir, float max_dist, Work
 // gather.wgsl:107-111
 inline V3 sky_color(V3 dir, V3 zenith, V3 horizon, float intensity) {
     float t = clampf(dir.y * 0.5f + 0.5f, 0.0f, 1.0f);
-    return mix3(horizon, zenith, std::pow(t, 0.5f)) * intensity;
+    return mix3(horizon, zenith, std::sqrt(t)) * intensity;
 }
 
 struct MatParams {
@@ -493,8 +517,10 @@ inline V3 sample_spec_dir(V3 rd, V3 n, float a, Rng &rng) {
     V3 t2 = cross(vh, t1);
     float r = std::sqrt(rng_f32(rng));
     float phi = 2.0f * PI * rng_f32(rng);
-    float x = r * std::cos(phi);
-    float y = r * std::sin(phi);
+    float sp, cp;
+    sincos_fixed(phi, sp, cp);
+    float x = r * cp;
+    float y = r * sp;
     float s = 0.5f * (1.0f + vh.z);
     float yy = (1.0f - s) * std::sqrt(fmx(0.0f, 1.0f - x * x)) + s * y;
     V3 hh = x * t1 + yy * t2 + std::sqrt(fmx(0.0f, 1.0f - x * x - yy * yy)) * vh;
@@ -651,7 +677,7 @@ void gather_pixel(const GatherCtx &g, uint32_t px, uint32_t py, PixelOut &out, W
 
             if (mat.kind == 2u) {  // gather.wgsl:421-436
                 float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
-                float f0s = std::pow(q, 2.0f);
+                float f0s = q * q;
                 float ct = std::fabs(dot(rd, shn));
                 float fr = fresnel_schlick(ct, mk(f0s, f0s, f0s)).x;
                 if (rng_f32(rng) < fr) {
@@ -907,7 +933,7 @@ void trace_photon(const Scene &sc, const rt_grid_params &gp, uint32_t photon_ind
         origin = center + d * R;
         dir = -d;
         float t = clampf(d.y * 0.5f + 0.5f, 0.0f, 1.0f);
-        power = mix3(ld(light.color), ld(light.data), std::pow(t, 0.5f)) * light.intensity;
+        power = mix3(ld(light.color), ld(light.data), std::sqrt(t)) * light.intensity;
     } else {
         return;
     }
@@ -941,7 +967,7 @@ void trace_photon(const Scene &sc, const rt_grid_params &gp, uint32_t photon_ind
         if (mat.tex_emissive != RT_TEX_NONE || length(ld(mat.emissive)) > 1e-4f || mat.kind == 3u) return;
         if (mat.kind == 2u) {
             float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
-            float f0s = std::pow(q, 2.0f);
+            float f0s = q * q;
             float cos_theta = std::fabs(dot(dir, face_normal));
             float fr = fresnel_schlick(cos_theta, mk(f0s, f0s, f0s)).x;
             if (rng_f32(rng) < fr) {
@@ -999,6 +1025,10 @@ inline uint32_t photon_key(const rt_grid_params &gp, const float *pos) {
 // C ABI of the oracle (ctypes)
 // ================================================================================================
 extern "C" {
+
+void oracle_sincos(const float *x, uint64_t n, float *s, float *c) {
+    for (uint64_t i = 0; i < n; ++i) sincos_fixed(x[i], s[i], c[i]);
+}
 
 uint32_t oracle_rng_sequence(uint32_t seed, uint32_t n, uint32_t *out_u32, float *out_f32) {
     Rng r = rng_init(seed);

@@ -119,7 +119,7 @@ __device__ bool photon_emit(const PhotonTraceParams &p, uint32_t photon_index, R
         origin = center + d * R;
         dir = -d;
         float t = clampf(d.y * 0.5f + 0.5f, 0.0f, 1.0f);
-        power = mix3(light.color, light.data, powf(t, 0.5f)) * light.intensity;
+        power = mix3(light.color, light.data, sqrtf(t)) * light.intensity;  // pow(t, 0.5), t in [0, 1]
     } else {
         return false;
     }
@@ -163,7 +163,7 @@ __device__ bool photon_bounce(const PhotonTraceParams &p, uint32_t photon_index,
     if (mat.tex_emissive != RT_TEX_NONE || len3(mat.emissive) > 1e-4f || mat.kind == 3u) return false;
     if (mat.kind == 2u) {
         float q = (mat.ior - 1.0f) / (mat.ior + 1.0f);
-        float f0s = powf(q, 2.0f);
+        float f0s = q * q;
         float ct = fabsf(dot(dir, face_normal));
         float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
         if (rng_f32(rng) < fr) {

@@ -80,7 +80,7 @@ __device__ __forceinline__ Accum load_acc(const WaveParams &p, uint32_t pix) {
 
 __device__ __forceinline__ f3 sky_color(f3 dir, f3 zenith, f3 horizon, float intensity) {
     float t = clampf(dir.y * 0.5f + 0.5f, 0.0f, 1.0f);
-    return mix3(horizon, zenith, powf(t, 0.5f)) * intensity;
+    return mix3(horizon, zenith, sqrtf(t)) * intensity;  // pow(t, 0.5) for t in [0, 1]
 }
 __device__ __forceinline__ float smith_g1(float nd, float a) {
     float k = a * 0.5f;
@@ -110,8 +110,10 @@ __device__ __forceinline__ f3 sample_spec_dir(f3 rd, f3 n, float a, Rng &rng) {
     f3 t2 = cross(vh, t1);
     float r = sqrtf(rng_f32(rng));
     float phi = 2.0f * kPi * rng_f32(rng);
-    float x = r * cosf(phi);
-    float y = r * sinf(phi);
+    float sp, cp;
+    sincos_fixed(phi, sp, cp);
+    float x = r * cp;
+    float y = r * sp;
     float s = 0.5f * (1.0f + vh.z);
     float yy = (1.0f - s) * sqrtf(fmaxf(0.0f, 1.0f - x * x)) + s * y;
     f3 hh = x * t1 + yy * t2 + sqrtf(fmaxf(0.0f, 1.0f - x * x - yy * yy)) * vh;
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
         for (uint32_t k = 0; k < steps; ++k) {
             if (kWide ? trav_step_warp4(st, has, false, stk, (uint32_t)kBlock, wl)
                       : trav_step_warp(st, has, false, stk, (uint32_t)kBlock, wl)) {
-                p.hit[slot] = make_float2(st.t, __uint_as_float(st.prim));
+                p.hit[slot] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
                 has = false;
             }
             if (!__any_sync(0xFFFFFFFFu, has)) break;
@@ -536,7 +538,7 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ W
                         alive = false;
                     } else if (mat.kind == 2u) {  // dielectric (gather.wgsl:421-436)
                         float qd = (mat.ior - 1.0f) / (mat.ior + 1.0f);
-                        float f0s = powf(qd, 2.0f);
+                        float f0s = qd * qd;
                         float ct = fabsf(dot(rd, shn));
                         float fr = fresnel_schlick(ct, mk3(f0s, f0s, f0s)).x;
                         if (rng_f32(rng) < fr) {
@@ -777,7 +779,7 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
     const DevScene &s = p.jobs[tag >> 17].scene;
     bool shadowed = !(st.t >= limit);
     if (shadowed && !s.any_hit_shadows) {
-        TriFull bt = load_tri(s, st.prim);
+        TriFull bt = load_tri(s, trav_hit_prim(st));
         Mat bm = load_mat(s, bt.material_id);
         if ((bm.flags & RT_MAT_FLAG_ALPHA_CUTOUT) != 0u && bm.tex_albedo != RT_TEX_NONE) {
             Bary b = barycentric(bt, xyz(o), xyz(d), st.t);
@@ -846,7 +848,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
             if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl)
                       : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
-                else p.hit[id] = make_float2(st.t, __uint_as_float(st.prim));
+                else p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
                 has = false;
             }
             if (!__any_sync(0xFFFFFFFFu, has)) break;

@@ -51,6 +51,28 @@ __device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
     float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
 }
+// sin and cos of one angle, and the integer powers the shaders write as pow(x, 2) and pow(x, 5).
+// WGSL leaves the accuracy of sin, cos and pow to the backend, so each is one fixed sequence of IEEE
+// operations, evaluated the same way in the oracle.  sin / cos: Cody-Waite reduction by pi/2 with a
+// two-part constant (W. J. Cody and W. Waite, Software Manual for the Elementary Functions, 1980;
+// 1.5703125 has 8 significant bits, so k * 1.5703125 is exact for |k| < 2^16), then the Taylor
+// series of sin (through x^9) and cos (through x^10) on [-pi/4, pi/4] in Horner form, whose
+// truncation error (below 3e-9) is under the float rounding; the quadrant picks the signs.
+__device__ __forceinline__ void sincos_fixed(float x, float &s, float &c) {
+    const float k = floorf(x * 0.636619772f + 0.5f);
+    const float r = (x - k * 1.5703125f) - k * 4.83826794e-4f;
+    const float z = r * r;
+    const float sr = r + r * z * (-(1.0f / 6.0f) + z * ((1.0f / 120.0f) + z * (-(1.0f / 5040.0f) + z * (1.0f / 362880.0f))));
+    const float cr = 1.0f - 0.5f * z +
+                     z * z * ((1.0f / 24.0f) + z * (-(1.0f / 720.0f) + z * ((1.0f / 40320.0f) + z * -(1.0f / 3628800.0f))));
+    const int q = (int)k & 3;
+    s = q == 0 ? sr : (q == 1 ? cr : (q == 2 ? -sr : -cr));
+    c = q == 0 ? cr : (q == 1 ? -sr : (q == 2 ? -cr : sr));
+}
+__device__ __forceinline__ float pow5(float x) {
+    const float x2 = x * x;
+    return x2 * x2 * x;
+}
 __device__ __forceinline__ uint32_t f2u_sat(float f) {
     if (!(f > 0.0f)) return 0u;
     if (f >= 4294967296.0f) return 0xFFFFFFFFu;
@@ -71,7 +93,7 @@ __device__ __forceinline__ f3 refract(f3 v, f3 n, float eta) {
     return perp + par;
 }
 __device__ __forceinline__ f3 fresnel_schlick(float cos_theta, f3 f0) {
-    float p = powf(clampf(1.0f - cos_theta, 0.0f, 1.0f), 5.0f);
+    float p = pow5(clampf(1.0f - cos_theta, 0.0f, 1.0f));
     return f0 + (mk3(1.0f, 1.0f, 1.0f) - f0) * p;
 }
 
@@ -99,7 +121,9 @@ __device__ __forceinline__ f3 sample_cosine_hemisphere(Rng &r) {
     float phi = 2.0f * kPi * u1;
     float ct = sqrtf(u2);
     float st = sqrtf(1.0f - u2);
-    return mk3(cosf(phi) * st, ct, sinf(phi) * st);
+    float sp, cp;
+    sincos_fixed(phi, sp, cp);
+    return mk3(cp * st, ct, sp * st);
 }
 __device__ __forceinline__ f3 to_world(f3 local, f3 n) {
     f3 up = fabsf(n.y) < 0.999f ? mk3(0.0f, 1.0f, 0.0f) : mk3(1.0f, 0.0f, 0.0f);
@@ -261,14 +285,17 @@ __device__ __forceinline__ float intersect_triangle(f3 ro, f3 rd, f3 v0, f3 v1, 
 // reference's slab test (gather.wgsl:71-75: (bmin - ro) / d, te <= ta && ta > 0 && te < t); leaf
 // children are intersected on the spot, internal children are visited nearest entry first with the
 // farther one pushed (a push is dropped once `stack_cap` entries are in use, as the reference drops
-// pushes at 63).  The tree is the reference's, so the closest hit is the reference's: only triangles
-// with exactly equal t may resolve to a different one of them.  The stack lives in shared memory, one
+// pushes at 63).  The tree is the reference's, so the closest hit is the reference's.  Triangles hit at
+// exactly equal t resolve to the lowest prim slot: leaves hold consecutive slot ranges with the left
+// child's below the right's (bvh.rs:159-219), so the reference's left-first walk, where the first
+// strictly smaller t wins, meets the lowest slot first.  During the walk st.prim holds the best prim
+// slot; trav_hit_prim gives the triangle index.  The stack lives in shared memory, one
 // 4-byte column per thread.  TravState makes the traversal resumable one record at a time, so
 // persistent warps can refill lanes whose ray finished.
 struct TravState {
     f3 ro, rd, inv;
     float t;
-    uint32_t prim, node, sp;
+    uint32_t prim, node, sp;  // prim: the prim slot of the best hit so far
     const float4 *cnodes, *tri_ord;  // the traversal layout of the ray's scene
     uint32_t cap;                    // stack entries this scene may use
 };
@@ -297,12 +324,12 @@ __device__ __forceinline__ TravState trav_begin(const DevScene &s, f3 ro, f3 rd,
 // their current record.  The triangles of the record's hit leaves are tested by the whole warp: the
 // leaf work of all lanes is laid out as one list (lane order, left leaf before right leaf, triangles
 // in leaf order), cut into rounds of 32 tests, one per lane, and each lane then folds the results of
-// its own tests in list order with the reference's rule (a test wins when its t is strictly below the
-// best so far), so a lane's result is what testing its leaves one by one gives.  Testing them one by
+// its own tests in list order (a test wins when its t is strictly below the best so far, or equal to it
+// with a lower prim slot), so a lane's result is what testing its leaves one by one gives.  Testing them one by
 // one in each lane instead leaves the warp waiting on the lanes with four-triangle leaves.
 //
-// Returns true for an active lane whose traversal has finished (st.t / st.prim hold the closest hit
-// below the starting st.t).  `any` lanes (occlusion queries) also finish at the first record whose
+// Returns true for an active lane whose traversal has finished (st.t and the prim slot st.prim hold
+// the closest hit below the starting st.t).  `any` lanes (occlusion queries) also finish at the first record whose
 // leaves hold a triangle below st.t; st.t is then the smallest such t of that record.  WarpLeaves is
 // per warp, and warp_leaves_set_ray must have stored a lane's ray before its first step.
 struct WarpLeaves {
@@ -324,8 +351,8 @@ __device__ __forceinline__ void warp_leaves_set_ray(WarpLeaves &w, const TravSta
 // The leaf tests of one traversal step for the whole warp: lane l has n_l tests (its run), laid out
 // in lane order and cut into rounds of 32; tri_of(owner, j) gives the prim slot of the owner's j-th
 // test (every lane calls it, with its own arguments).  Each lane folds its own results in run order
-// into st.t / st.prim (a test wins when its t is strictly below the best so far) and returns whether
-// any of them won.
+// into st.t / st.prim (a test wins when its t is strictly below the best so far, or equal to it with a
+// lower prim slot) and returns whether any of them won.
 template <typename TriOf>
 __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, WarpLeaves &w, TriOf tri_of) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -377,7 +404,7 @@ __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, Warp
                     }
                 }
             }
-            prim = __float_as_uint(v0.w);
+            prim = tri;
         }
         w.t[lane] = t;
         w.prim[lane] = prim;
@@ -385,9 +412,10 @@ __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, Warp
         if (mine) {
             for (uint32_t k = lo - base; k < hi - base; ++k) {
                 const float tk = w.t[k];
-                if (tk < st.t) {
+                const uint32_t sk = w.prim[k];
+                if (tk < st.t || (tk == st.t && sk < st.prim)) {
                     st.t = tk;
-                    st.prim = w.prim[k];
+                    st.prim = sk;
                     found = true;
                 }
             }
@@ -460,7 +488,7 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
 // record with the same slab test, queues the hit leaves' triangles (child order) for the warp's leaf
 // rounds, and visits the hit internal children nearest entry first (the others pushed, farthest
 // first; the stack holds every pending entry).  Same results as the two-wide walk: the closest hit
-// below the starting st.t, only triangles with exactly equal t may resolve to another of them.
+// below the starting st.t, ties resolved to the lowest prim slot as in the two-wide walk.
 __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
                                                 WarpLeaves &w) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -543,6 +571,12 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
         return first + (j - at);
     });
     return active && (exhausted || (any && found));
+}
+
+// The triangle index of a finished closest-hit traversal (st.prim holds the hit's prim slot; a miss
+// gives 0).
+__device__ __forceinline__ uint32_t trav_hit_prim(const TravState &st) {
+    return st.t < kInf ? __float_as_uint(__ldg(st.tri_ord + 3ull * st.prim).w) : 0u;
 }
 
 struct Bary {

@@ -1,11 +1,13 @@
 """Parity of the sm_103a kernels (through the C ABI) with the oracle on the same inputs.
 
 Tolerances (floating point, written here as the parity bar states them):
-  * accumulated radiance: |gpu - oracle| <= 1e-3 |oracle| + 1e-6 on at least 99.9% of channels; the
-    rest are paths that diverged on an ulp-level difference (CUDA's and glibc's sinf/cosf/powf/expf
-    differ by an ulp or two, which can flip a silhouette hit or a lobe choice);
-  * stage kernels on identical inputs: 1e-5 relative (denoise: exp/pow per tap), bit-exact where no
-    transcendental function is involved (composite), +-1 on rgba8 bytes (tonemap pow);
+  * accumulated radiance: |gpu - oracle| <= 1e-3 |oracle| + 1e-6 on at least 99.9% of channels (the
+    path's sin / cos / pow are one fixed IEEE sequence on both backends and equal-t hits resolve to
+    the lowest prim slot, so paths do not diverge; the margin is for float evaluation-order
+    differences);
+  * stage kernels on identical inputs: 1e-5 relative (denoise: CUDA's and glibc's exp / pow per tap
+    differ by an ulp or two), bit-exact where no transcendental function is involved (composite),
+    +-1 on rgba8 bytes (tonemap pow);
   * integer work (cell keys, counts, offsets, slot order): bit-exact.
 """
 import numpy as np
@@ -63,32 +65,6 @@ def test_cornell_config1_accumulation(gpu, orc):
     assert r.sample_count() == 16
     tm = r.read_tonemapped()
     assert (np.abs(tm.astype(int) - o.output.astype(int)) <= 1).mean() >= FRAC
-
-
-def test_config1_error_against_a_converged_render(gpu, orc):
-    """The RMSE of config 1's 16-sample image against a converged (4096 spp) render is the same for the
-    CUDA path and the oracle, and it falls with more samples (the estimator converges to one image)."""
-    scene = rt.Scene.cornell555()
-    cam = scene.default_camera()
-
-    def gpu_image(spp, frames):
-        cfg = rt.RenderConfig(width=128, height=128, spp=spp, accumulate_frames=frames, enable_denoise=False)
-        r = rt.Renderer(scene, cfg)
-        r.update_camera(cam)
-        r.render_frames(frames)
-        img = r.read_accumulation()[..., :3].astype(np.float64)
-        r.close()
-        return img
-
-    converged = gpu_image(1, 4096)
-    cfg16 = rt.RenderConfig(width=128, height=128, spp=1, accumulate_frames=16, enable_denoise=False)
-    r, o = render_both(orc, scene, cfg16, 16)
-    rmse = lambda a: float(np.sqrt(np.mean((a - converged) ** 2)))  # noqa: E731
-    e_gpu = rmse(r.read_accumulation()[..., :3].astype(np.float64))
-    e_orc = rmse(o.accum[..., :3].astype(np.float64))
-    assert abs(e_gpu - e_orc) <= 0.01 * e_orc, (e_gpu, e_orc)
-    e_64 = rmse(gpu_image(1, 64))
-    assert e_64 < 0.7 * e_gpu, (e_64, e_gpu)  # ~1/sqrt(spp): 64 samples halve the error of 16
 
 
 def test_first_frame_buffers(gpu, orc):
@@ -211,7 +187,7 @@ def test_photon_map_and_denoise_cornell(gpu, orc):
     o = oracle_for(orc, scene, cfg, cam)
     o.rebuild_photons()
     # the traces agree slot by slot (float tolerance; a diverged photon path shows as a mismatch)
-    assert match_frac(gpu_ph.view(np.float32), o.photons.view(np.float32), rtol=1e-4, atol=1e-4) >= 0.995
+    assert match_frac(gpu_ph.view(np.float32), o.photons.view(np.float32), rtol=1e-4, atol=1e-4) >= FRAC
     # the grid is exact on an identical photon buffer
     o.load_photons(gpu_ph)
     counts, meta = r.read_photon_grid()

@@ -51,6 +51,25 @@ def test_rng_f32_can_reach_one():
     assert np.float32(np.uint32(0xFFFFFF7F)) / np.float32(4294967296.0) < 1.0
 
 
+def test_fixed_sincos_error_bound(orc):
+    """The sampling angles' sin / cos (one fixed IEEE sequence on both backends) against float64.
+
+    The angles are 2*pi*u with u = rng_f32 in [0, 1] (common.wgsl:60-74, the VNDF disk of
+    gather.wgsl:230-256); WGSL itself only asks for 2^-11 absolute error.  The bound here is 2 ulp of
+    1.0 (2.4e-7) absolute over every reachable angle of a dense sweep, plus the endpoints."""
+    u = np.concatenate([np.linspace(0.0, 1.0, 1 << 20, dtype=np.float32),
+                        np.float32([0.0, 0.25, 0.5, 0.75, 1.0, 1e-30, 0.9999999])])
+    phi = np.float32(2.0) * np.float32(np.pi) * u
+    s, c = orc.sincos(phi)
+    x = phi.astype(np.float64)
+    assert np.abs(s - np.sin(x)).max() < 2.4e-7
+    assert np.abs(c - np.cos(x)).max() < 2.4e-7
+    # sin^2 + cos^2 stays 1 within float rounding, and the quadrant signs are right
+    assert np.abs(s.astype(np.float64) ** 2 + c.astype(np.float64) ** 2 - 1.0).max() < 5e-7
+    assert (np.sign(s[(x > 1e-3) & (x < np.pi - 1e-3)]) > 0).all()
+    assert (np.sign(c[(x > np.pi / 2 + 1e-3) & (x < 1.5 * np.pi - 1e-3)]) < 0).all()
+
+
 def test_pixel_seed_formula(orc):
     # gather.wgsl:262-263: rng_init((y*W + x + frame*2654435761) * 1664525 + 1013904223)
     W = 256
