@@ -158,16 +158,34 @@ def make_config(w: dict):
 
 
 # ------------------------------------------------------------------------------------------------
-# CPU legs (oracle): bounded samples of the same frames
+# CPU legs (oracle): bounded samples of the same frames.  They load only the oracle: the scene is
+# the one the oracle generates and indexes itself (byte-identical to the backend's, checked by
+# tests/test_oracle_scene.py), so no product code runs on the reference's path.
 # ------------------------------------------------------------------------------------------------
-def cpu_sample(scene, cfg, cam, seconds: float, threads: int, frames: int = 1):
-    """Times the oracle on row bands of `frames` consecutive frames, sized to ~`seconds` in total.
-    Returns (segments/s, sample description, per-ray work counters)."""
+def oracle_workload(w: dict):
+    """(oracle scene, oracle config) of a workload."""
     import oracle
 
-    u = oracle.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, cfg.width, cfg.height, cam.near,
-                              cam.aperture, cam.focus_dist)
-    o = oracle.OracleRenderer(scene.describe(), cfg, u, threads=threads)
+    if w["scene"] == "cornell":
+        scene = oracle.OracleScene.cornell555()
+    else:
+        scene = oracle.OracleScene.icosphere_room(w["level"], w["seed"], w["sigma"], w["tex"])
+    cfg = oracle.Config(width=w["width"], height=w["height"], spp=w["spp"], accumulate_frames=w["accumulate_frames"],
+                        enable_denoise=w["denoise"], enable_photon_map=bool(w["photons"]),
+                        photon_count=max(w["photons"], 1), max_bounces=w["max_bounces"])
+    return scene, cfg
+
+
+def cpu_sample(scene, cfg, seconds: float, threads: int, frames: int = 1):
+    """Times the oracle on row bands of `frames` consecutive frames of its own scene (default
+    camera), sized to ~`seconds` in total.  Returns (segments/s, sample description, per-ray work
+    counters)."""
+    import oracle
+
+    c = scene.camera()
+    u = oracle.camera_uniform(tuple(c.position), tuple(c.look_at), tuple(c.up), c.fov_degrees, cfg.width, cfg.height,
+                              c.near_plane, c.aperture, c.focus_dist)
+    o = oracle.OracleRenderer(scene, cfg, u, threads=threads)
     # calibrate on a small band
     rows = max(1, min(cfg.height, 4 * max(threads, 1)))
     t0 = time.perf_counter()
@@ -220,17 +238,15 @@ def run_reference(args, w):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    scene = make_scene(w)
-    cfg = make_config(w)
-    cam = scene.default_camera()
+    scene, cfg = oracle_workload(w)
     # warm-up samples, then K timed samples (one row band each)
     per_step = max(0.05, min(20.0, args.ref_seconds / max(args.steps + args.warmup, 1)))
     for _ in range(args.warmup):
-        cpu_sample(scene, cfg, cam, per_step / 4, threads)
+        cpu_sample(scene, cfg, per_step / 4, threads)
     vals, descs = [], []
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        v, d, _ = cpu_sample(scene, cfg, cam, per_step, threads)
+        v, d, _ = cpu_sample(scene, cfg, per_step, threads)
         vals.append(v)
         descs.append(d)
     wall = time.perf_counter() - t_all
@@ -238,12 +254,14 @@ def run_reference(args, w):
     line = {"impl": "reference", "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: v for k, v in w.items()}, "l2": "inputs larger than L2"},
+            "config": {"workload": args.workload, **{k: v for k, v in w.items()}, "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}"},
             "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
                              "sample": descs[0]},
             "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "reference = the oracle's C++ restatement of the WGSL path on the host cores; the Rust/wgpu "
-                    "reference cannot run here (no Rust toolchain, no graphics stack)"}
+            "note": "reference = the oracle's C++ restatement of the WGSL path on the host cores, on the scene the "
+                    "oracle generates and indexes itself (no product library is loaded); the Rust/wgpu reference "
+                    "cannot run here (no Rust toolchain, no graphics stack)"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -629,7 +647,9 @@ def run_ours(args, w):
         resolve_ms = s1.ms_resolve_sum / max(s1.timed_frames, 1)
         # CPU baseline (oracle on this host's cores, bounded sample) and the per-ray work it counts.
         threads = os.cpu_count() or 1
-        cpu_val, cpu_desc, work = cpu_sample(scene, cfg, cam, args.cpu_seconds, threads)
+        oscene, ocfg = oracle_workload(w)
+        cpu_val, cpu_desc, work = cpu_sample(oscene, ocfg, args.cpu_seconds, threads)
+        del oscene
         seg_per_frame = segments / max(args.steps, 1)
         shd_per_frame = shadow / max(args.steps, 1)
         rays = seg_per_frame + shd_per_frame

@@ -60,6 +60,27 @@ class TonemapParams(C.Structure):
                 ("marker", C.c_float * 4)]
 
 
+class TextureArray(C.Structure):
+    _fields_ = [("rgba8", C.c_void_p), ("width", u32), ("height", u32), ("layers", u32), ("_pad", u32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("triangles", C.c_void_p), ("triangle_count", C.c_uint64), ("bvh_nodes", C.c_void_p),
+                ("bvh_node_count", C.c_uint64), ("bvh_prims", C.c_void_p), ("bvh_prim_count", C.c_uint64),
+                ("materials", C.c_void_p), ("material_count", C.c_uint64), ("lights", C.c_void_p),
+                ("light_count", C.c_uint64), ("tex_albedo", TextureArray), ("tex_mr", TextureArray),
+                ("tex_emissive", TextureArray), ("tex_normal", TextureArray), ("bounds_min", f3),
+                ("bounds_max", f3), ("has_bounds", u32), ("_pad", u32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", f3), ("look_at", f3), ("up", f3), ("fov_degrees", C.c_float), ("near_plane", C.c_float),
+                ("aperture", C.c_float), ("focus_dist", C.c_float)]
+
+
+BVH_NODE_DTYPE = np.dtype([("bbox_min", "<f4", 3), ("left_first", "<u4"), ("bbox_max", "<f4", 3),
+                           ("right_child", "<u4"), ("prim_count", "<u4"), ("_pad", "<f4", 3)])
+
 PHOTON_DTYPE = np.dtype([("position", "<f4", 3), ("_pad0", "<f4"), ("power", "<f4", 3), ("_pad1", "<f4"),
                          ("incident", "<f4", 3), ("_pad2", "<f4"), ("normal", "<f4", 3), ("_pad3", "<f4")])
 
@@ -80,6 +101,13 @@ _PROTOS = {
     "oracle_camera_to_uniform": (None, [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, u32, u32,
                                         C.POINTER(CameraUniform)]),
     "oracle_derive_grid": (None, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(GridParams), C.POINTER(C.c_float)]),
+    "oracle_scene_cornell555": (vp, []),
+    "oracle_scene_icosphere_room": (vp, [u32, C.c_uint64, C.c_float, u32]),
+    "oracle_scene_from_arrays": (vp, [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64, vp]),
+    "oracle_scene_describe": (None, [vp, C.POINTER(SceneDesc)]),
+    "oracle_scene_camera": (None, [vp, C.POINTER(Camera)]),
+    "oracle_scene_destroy": (None, [vp]),
+    "oracle_bvh_build": (C.c_uint64, [vp, vp, vp, C.c_uint64, vp, vp]),
 }
 
 _lib: C.CDLL | None = None
@@ -211,6 +239,107 @@ def photon_grid(photons: np.ndarray, gp: GridParams):
     return counts, meta, srt, int(n)
 
 
+class Config:
+    """The RenderConfig fields the oracle reads (rustracer-renderer/src/lib.rs:21-65 and its defaults,
+    plus the max_bounces / denoise_passes / grid extensions; 0 means the reference's value)."""
+
+    def __init__(self, **kw):
+        self.width, self.height, self.photon_count, self.spp = 800, 600, 1_000_000, 1
+        self.exposure, self.gamma = 1.0, 2.2
+        self.light_emission, self.point_light_emission = (1.0, 1.0, 1.0), (1.0, 1.0, 1.0)
+        self.accumulate_frames, self.enable_photon_map, self.enable_denoise = 0, False, True
+        self.photon_debug, self.debug_view, self.photon_scale, self.photon_radius = False, 0, 0.02, 0.5
+        self.ambient = 0.03
+        self.max_bounces, self.denoise_passes, self.grid_max_dim, self.photon_radius_mode = 0, 0, 0, 0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"unknown config field {k}")
+            setattr(self, k, v)
+
+
+class OracleScene:
+    """A scene generated and indexed by the oracle itself (oracle/scene.cpp): its own flattening and
+    SAH BVH build, so the oracle's traversal does not depend on the CUDA backend's host code."""
+
+    def __init__(self, handle: int, keep=None):
+        if not handle:
+            raise RuntimeError("the oracle rejected the scene arguments")
+        self._h = C.c_void_p(handle)
+        self._keep = keep
+        self.desc = SceneDesc()
+        load().oracle_scene_describe(self._h, C.byref(self.desc))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().oracle_scene_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def cornell555() -> "OracleScene":
+        return OracleScene(load().oracle_scene_cornell555())
+
+    @staticmethod
+    def icosphere_room(level: int = 8, seed: int = 0, sigma: float = 0.02, tex_size: int = 1024) -> "OracleScene":
+        return OracleScene(load().oracle_scene_icosphere_room(level, seed, sigma, tex_size))
+
+    @staticmethod
+    def from_arrays(triangles: np.ndarray, materials: np.ndarray, lights: np.ndarray,
+                    textures=None) -> "OracleScene":
+        """triangles / materials / lights: arrays of the 128 / 64 / 64-byte records; textures: up to
+        four (layers, h, w, 4) uint8 arrays or None per role (albedo, MR, emissive, normal)."""
+        t, m, li = (np.ascontiguousarray(x) for x in (triangles, materials, lights))
+        tex = (TextureArray * 4)()
+        keep = [t, m, li]
+        for r, arr in enumerate(textures or []):
+            if arr is None or arr.size == 0:
+                continue
+            a = np.ascontiguousarray(arr, np.uint8)
+            if a.ndim == 3:
+                a = a[None]
+            keep.append(a)
+            tex[r].rgba8 = a.ctypes.data
+            tex[r].layers, tex[r].height, tex[r].width = a.shape[0], a.shape[1], a.shape[2]
+        h = load().oracle_scene_from_arrays(_p(t), len(t), _p(m), len(m), _p(li) if len(li) else None, len(li), tex)
+        return OracleScene(h, keep)
+
+    def camera(self) -> Camera:
+        c = Camera()
+        load().oracle_scene_camera(self._h, C.byref(c))
+        return c
+
+    def arrays(self) -> dict[str, np.ndarray]:
+        """Byte copies of the flattened arrays (triangles / materials / lights as raw records)."""
+        d = self.desc
+
+        def raw(ptr, n, size):
+            if n == 0:
+                return np.zeros((0, size), np.uint8)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_uint8)), shape=(n * size,)).reshape(n, size).copy()
+
+        out = {"triangles": raw(d.triangles, d.triangle_count, 128), "materials": raw(d.materials, d.material_count, 64),
+               "lights": raw(d.lights, d.light_count, 64),
+               "bvh_nodes": raw(d.bvh_nodes, d.bvh_node_count, 48).view(BVH_NODE_DTYPE).reshape(-1),
+               "bvh_prims": raw(d.bvh_prims, d.bvh_prim_count, 4).view(np.uint32).reshape(-1)}
+        for name in ("tex_albedo", "tex_mr", "tex_emissive", "tex_normal"):
+            t = getattr(d, name)
+            n = t.width * t.height * t.layers * 4
+            out[name] = (np.ctypeslib.as_array(C.cast(t.rgba8, C.POINTER(C.c_uint8)), shape=(n,)).copy()
+                         if t.layers and t.rgba8 else np.zeros(0, np.uint8))
+        out["bounds"] = (np.array(d.bounds_min, np.float32), np.array(d.bounds_max, np.float32), int(d.has_bounds))
+        return out
+
+
+def bvh_build(centroids: np.ndarray, bmin: np.ndarray, bmax: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The oracle's SAH build on raw primitive centroids and boxes: (nodes, prim indices)."""
+    c, lo, hi = (np.ascontiguousarray(x, np.float32).reshape(-1, 3) for x in (centroids, bmin, bmax))
+    n = len(c)
+    nodes = np.zeros(max(2 * n, 1), BVH_NODE_DTYPE)
+    prims = np.zeros(max(n, 1), np.uint32)
+    k = load().oracle_bvh_build(_p(c), _p(lo), _p(hi), n, _p(nodes), _p(prims))
+    return nodes[:k].copy(), prims[:n].copy()
+
+
 class OracleRenderer:
     """CPU driver of the reference's frame schedule over the oracle kernels.
 
@@ -219,6 +348,9 @@ class OracleRenderer:
     """
 
     def __init__(self, scene_desc, config, camera_uniform=None, threads: int = 0):
+        if isinstance(scene_desc, OracleScene):
+            self.scene = scene_desc
+            scene_desc = scene_desc.desc
         self.desc = scene_desc
         self.cfg = config
         self.threads = threads

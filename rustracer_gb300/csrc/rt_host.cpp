@@ -46,8 +46,9 @@ Vec3 normalize(Vec3 a) {
 // BVH (bvh.rs:120-336).  Same algorithm: 12 centroid bins per axis, bins carry the union of the full
 // primitive AABBs, split cost 1 + (A_l n_l + A_r n_r) / A, leaf when that is not below n, at most 4
 // primitives per leaf, children emitted before parents and the array reversed so the root is node 0.
-// The partition is a selection by (centroid[axis], primitive index): the reference's
-// select_nth_unstable_by leaves the order of equal centroids unspecified, this one fixes it.
+// The partition is a selection by (centroid[axis], primitive index) and a leaf lists its primitives
+// in index order: the reference's select_nth_unstable_by leaves both orders unspecified, this one
+// fixes them.
 // ------------------------------------------------------------------------------------------------
 namespace {
 
@@ -170,6 +171,9 @@ struct Builder {
         node.bbox_min[0] = bb.mn.x; node.bbox_min[1] = bb.mn.y; node.bbox_min[2] = bb.mn.z;
         node.bbox_max[0] = bb.mx.x; node.bbox_max[1] = bb.mx.y; node.bbox_max[2] = bb.mx.z;
         if (!split) {
+            // A leaf's primitives in index order: the selection leaves their order unspecified, and
+            // it decides which of two triangles hit at exactly equal t the traversal reports.
+            std::sort(prims.begin() + start, prims.begin() + end);
             node.left_first = (uint32_t)start;
             node.right_child = 0;
             node.prim_count = (uint32_t)count;
@@ -1125,8 +1129,12 @@ extern "C" int rt_scene_create_icosphere_room(uint32_t level, uint64_t seed, flo
         double u = rng.uniform();
         rt_material m;
         if (u < 0.60) {
-            m = mat_lambertian((float)(0.2 + 0.6 * rng.uniform()), (float)(0.2 + 0.6 * rng.uniform()),
-                               (float)(0.2 + 0.6 * rng.uniform()));
+            // one declaration per draw: the order of the draws must not depend on the compiler's
+            // order of evaluating call arguments
+            const float r = (float)(0.2 + 0.6 * rng.uniform());
+            const float g = (float)(0.2 + 0.6 * rng.uniform());
+            const float b = (float)(0.2 + 0.6 * rng.uniform());
+            m = mat_lambertian(r, g, b);
         } else if (u < 0.85) {
             float r = (float)(0.5 + 0.45 * rng.uniform()), g = (float)(0.5 + 0.45 * rng.uniform()),
                   b = (float)(0.5 + 0.45 * rng.uniform());

@@ -3,7 +3,8 @@
     python tests/golden/make_golden.py
 
 The reference (Rust + WGSL on wgpu) cannot run on this machine, so these vectors pin the oracle's
-restatement against regressions; the independent checks live in tests/test_oracle_pins.py.
+restatement against regressions; the independent checks live in tests/test_oracle_pins.py.  Only the
+oracle runs here: the scenes are the oracle's own (oracle/scene.cpp).
 """
 from __future__ import annotations
 
@@ -17,21 +18,24 @@ ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
-import rustracer_gb300 as rt  # noqa: E402
 
 RNG_SEEDS = [0, 1, 12345, 0xFFFFFFFF, 2654435761, 1013904223]
 
 
-def oracle_render(scene, cfg, frames, cam=None):
-    cam = cam or scene.default_camera()
-    u = oracle.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, cfg.width, cfg.height, cam.near,
-                              cam.aperture, cam.focus_dist)
-    o = oracle.OracleRenderer(scene.describe(), cfg, u, threads=1)
+def oracle_render(scene, cfg, frames):
+    o = oracle.OracleRenderer(scene, cfg, camera_of(scene, cfg), threads=1)
     if cfg.enable_photon_map:
         o.rebuild_photons()
     for _ in range(frames):
         o.record_frame()
     return o
+
+
+def camera_of(scene, cfg):
+    """The camera uniform of an oracle scene's default camera at the config's size."""
+    c = scene.camera()
+    return oracle.camera_uniform(tuple(c.position), tuple(c.look_at), tuple(c.up), c.fov_degrees, cfg.width,
+                                 cfg.height, c.near_plane, c.aperture, c.focus_dist)
 
 
 def golden_inputs_denoise():
@@ -68,21 +72,21 @@ def main() -> None:
     np.savez_compressed(HERE / "rng.npz", seeds=np.array(RNG_SEEDS, np.uint32), u32=seqs)
 
     # Cornell (config-1 scene) at 32x32, spp 2, denoise on, 4 frames
-    sc = rt.Scene.cornell555()
-    cfg = rt.RenderConfig(width=32, height=32, spp=2, accumulate_frames=4, enable_denoise=True)
+    sc = oracle.OracleScene.cornell555()
+    cfg = oracle.Config(width=32, height=32, spp=2, accumulate_frames=4, enable_denoise=True)
     o = oracle_render(sc, cfg, 4)
     np.savez_compressed(HERE / "cornell_32x32.npz", accum=o.accum, output=o.output, frame=o.frame,
                         moments=o.moments, gbuffer=o.gbuffer, counters=o.counters)
     out["cornell"] = o.counters.tolist()
 
     # textured icosphere room, all material kinds, depth 8
-    ico = rt.Scene.icosphere_room(level=2, seed=3, sigma=0.02, tex_size=16)
-    cfg2 = rt.RenderConfig(width=24, height=16, spp=3, accumulate_frames=2, enable_denoise=False, max_bounces=8)
+    ico = oracle.OracleScene.icosphere_room(2, 3, 0.02, 16)
+    cfg2 = oracle.Config(width=24, height=16, spp=3, accumulate_frames=2, enable_denoise=False, max_bounces=8)
     o2 = oracle_render(ico, cfg2, 2)
     np.savez_compressed(HERE / "icosphere_24x16.npz", accum=o2.accum, counters=o2.counters)
 
     # photon trace of the Cornell box, 512 photons (the reference's GPU smoke-test size)
-    cfg3 = rt.RenderConfig(width=8, height=8, enable_photon_map=True, photon_count=512, spp=1)
+    cfg3 = oracle.Config(width=8, height=8, enable_photon_map=True, photon_count=512, spp=1)
     o3 = oracle_render(sc, cfg3, 0)
     np.savez_compressed(HERE / "photons_cornell_512.npz", photons=o3.photons.view(np.uint8),
                         counts=o3.grid_counts, meta=o3.grid_meta)

@@ -23,16 +23,19 @@ pytestmark = pytest.mark.gpu
 RTOL, ATOL, FRAC = 1e-3, 1e-6, 0.999
 
 
+def oracle_on(orc, oscene, cfg):
+    """The oracle rendering a scene it generated and indexed itself (equal to the backend's scene byte
+    for byte: test_oracle_scene.py), from the scene's default camera."""
+    c = oscene.camera()
+    u = orc.camera_uniform(tuple(c.position), tuple(c.look_at), tuple(c.up), c.fov_degrees, cfg.width, cfg.height,
+                           c.near_plane, c.aperture, c.focus_dist)
+    return orc.OracleRenderer(oscene, cfg, u)
+
+
 def close(a, b, rtol=RTOL, atol=ATOL):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return np.abs(a - b) <= rtol * np.abs(b) + atol
-
-
-def oracle_for(orc, scene, cfg, cam):
-    u = orc.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, cfg.width, cfg.height, cam.near,
-                           cam.aperture, cam.focus_dist)
-    return orc.OracleRenderer(scene.describe(), cfg, u)
 
 
 def test_config2_accumulated_32_frames(gpu, orc):
@@ -51,7 +54,7 @@ def test_config2_accumulated_32_frames(gpu, orc):
     bands = [(int(a), int(a) + 2) for a in starts]
     rows = np.concatenate([np.arange(a, b) for a, b in bands])
     assert len(np.unique(rows)) == 54
-    o = oracle_for(orc, s, cfg, cam)
+    o = oracle_on(orc, orc.OracleScene.icosphere_room(8, 0, 0.02, 1024), cfg)
     for _ in range(32):
         o.record_frame(rows=bands)
     ok = close(acc[rows], o.accum[rows])
@@ -80,7 +83,7 @@ def test_config3_full_size_photons_denoise(gpu, orc):
     assert np.isfinite(acc).all()
     r.close()
 
-    o = oracle_for(orc, s, cfg, cam)
+    o = oracle_on(orc, orc.OracleScene.cornell555(), cfg)
     o.rebuild_photons()  # the oracle's own photon trace and counting sort
     a = ph.view(np.float32).reshape(len(ph), -1)
     b = o.photons.view(np.float32).reshape(len(ph), -1)
@@ -121,8 +124,10 @@ def test_config1_converged_oracle_render(gpu, orc):
         r.close()
         return img
 
+    oscene = orc.OracleScene.cornell555()
+
     def oracle_image(frames):
-        o = oracle_for(orc, scene, cfg_for(frames), cam)
+        o = oracle_on(orc, oscene, cfg_for(frames))
         for _ in range(frames):
             o.record_frame()
         return o.accum[..., :3].astype(np.float64)

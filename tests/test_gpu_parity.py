@@ -10,6 +10,8 @@ Tolerances (floating point, written here as the parity bar states them):
     +-1 on rgba8 bytes (tonemap pow);
   * integer work (cell keys, counts, offsets, slot order): bit-exact.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -28,10 +30,28 @@ def match_frac(a, b, rtol=RTOL, atol=ATOL):
     return float(ok.mean())
 
 
+def oracle_scene(orc, scene):
+    """The oracle's copy of a backend scene: the flattened triangles, materials, lights and textures
+    handed over and indexed by the oracle's own BVH build, so the oracle never walks the backend's
+    tree (the builds agree byte for byte on the CPU: test_oracle_scene.py)."""
+    a = scene.arrays()
+    d = scene.describe()
+    tex = []
+    for name in ("tex_albedo", "tex_mr", "tex_emissive", "tex_normal"):
+        t = getattr(d, name)
+        n = t.width * t.height * t.layers * 4
+        tex.append(np.ctypeslib.as_array(C.cast(t.rgba8, C.POINTER(C.c_uint8)), shape=(n,)).reshape(
+            t.layers, t.height, t.width, 4).copy() if t.layers else None)
+    o = orc.OracleScene.from_arrays(a["triangles"], a["materials"], a["lights"], tex)
+    lo, hi, has = o.arrays()["bounds"]
+    assert has == d.has_bounds and (not has or (tuple(lo) == tuple(d.bounds_min) and tuple(hi) == tuple(d.bounds_max)))
+    return o
+
+
 def oracle_for(orc, scene, cfg, cam):
     u = orc.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, cfg.width, cfg.height, cam.near,
                            cam.aperture, cam.focus_dist)
-    return orc.OracleRenderer(scene.describe(), cfg, u)
+    return orc.OracleRenderer(oracle_scene(orc, scene), cfg, u)
 
 
 def render_both(orc, scene, cfg, frames, cam=None, photons=False):

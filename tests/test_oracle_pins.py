@@ -9,13 +9,13 @@ rest of the path parity is unpinned by the reference, so the checks here are:
   * photon-grid invariants against a numpy stable sort;
   * golden vectors: integers bit-exact, floats within 1e-5 relative (libm may differ by an ulp
     between host architectures).
+Everything here runs the oracle alone, on the scenes it generates itself.
 """
 from pathlib import Path
 
 import numpy as np
 import pytest
 
-import rustracer_gb300 as rt
 
 G = Path(__file__).resolve().parent / "golden"
 M32 = 0xFFFFFFFF
@@ -137,19 +137,22 @@ def test_denoise_constant_image_is_identity(orc):
     assert np.allclose(out, frame, rtol=1e-6, atol=0)
 
 
+def camera_of(orc, scene, cfg):
+    c = scene.camera()
+    return orc.camera_uniform(tuple(c.position), tuple(c.look_at), tuple(c.up), c.fov_degrees, cfg.width,
+                              cfg.height, c.near_plane, c.aperture, c.focus_dist)
+
+
 def close(a, b, rtol=1e-5, frac=0.999):
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
     return float((np.abs(a - b) <= rtol * np.abs(b) + 1e-7).mean()) >= frac
 
 
-def test_golden_cornell_render(lib, orc):
+def test_golden_cornell_render(orc):
     d = np.load(G / "cornell_32x32.npz")
-    sc = rt.Scene.cornell555()
-    cfg = rt.RenderConfig(width=32, height=32, spp=2, accumulate_frames=4, enable_denoise=True)
-    cam = sc.default_camera()
-    u = orc.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, 32, 32, cam.near, cam.aperture,
-                           cam.focus_dist)
-    o = orc.OracleRenderer(sc.describe(), cfg, u, threads=2)
+    sc = orc.OracleScene.cornell555()
+    cfg = orc.Config(width=32, height=32, spp=2, accumulate_frames=4, enable_denoise=True)
+    o = orc.OracleRenderer(sc, cfg, camera_of(orc, sc, cfg), threads=2)
     for _ in range(4):
         o.record_frame()
     assert close(o.accum, d["accum"]) and close(o.gbuffer, d["gbuffer"]) and close(o.moments, d["moments"])
@@ -157,26 +160,21 @@ def test_golden_cornell_render(lib, orc):
     assert np.abs(o.counters.astype(np.int64) - d["counters"].astype(np.int64)).max() <= 0.001 * d["counters"].max()
 
 
-def test_golden_icosphere_render(lib, orc):
+def test_golden_icosphere_render(orc):
     d = np.load(G / "icosphere_24x16.npz")
-    sc = rt.Scene.icosphere_room(level=2, seed=3, sigma=0.02, tex_size=16)
-    cfg = rt.RenderConfig(width=24, height=16, spp=3, accumulate_frames=2, enable_denoise=False, max_bounces=8)
-    cam = sc.default_camera()
-    u = orc.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, 24, 16, cam.near, cam.aperture,
-                           cam.focus_dist)
-    o = orc.OracleRenderer(sc.describe(), cfg, u, threads=2)
+    sc = orc.OracleScene.icosphere_room(2, 3, 0.02, 16)
+    cfg = orc.Config(width=24, height=16, spp=3, accumulate_frames=2, enable_denoise=False, max_bounces=8)
+    o = orc.OracleRenderer(sc, cfg, camera_of(orc, sc, cfg), threads=2)
     for _ in range(2):
         o.record_frame()
     assert close(o.accum, d["accum"])
 
 
-def test_golden_photon_trace(lib, orc):
+def test_golden_photon_trace(orc):
     d = np.load(G / "photons_cornell_512.npz")
-    sc = rt.Scene.cornell555()
-    cfg = rt.RenderConfig(width=8, height=8, enable_photon_map=True, photon_count=512, spp=1)
-    cam = sc.default_camera()
-    u = orc.camera_uniform(cam.position, cam.look_at, cam.up, cam.fov_degrees, 8, 8)
-    o = orc.OracleRenderer(sc.describe(), cfg, u, threads=2)
+    sc = orc.OracleScene.cornell555()
+    cfg = orc.Config(width=8, height=8, enable_photon_map=True, photon_count=512, spp=1)
+    o = orc.OracleRenderer(sc, cfg, camera_of(orc, sc, cfg), threads=2)
     o.rebuild_photons()
     ref = d["photons"].view(orc.PHOTON_DTYPE)
     assert close(o.photons.view(np.float32), ref.view(np.float32), frac=0.995)
