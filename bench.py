@@ -269,18 +269,50 @@ def run_reference(args, w):
 # ------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------
-def load_traffic(workload: str) -> float | None:
-    """DRAM bytes per gather launch from the committed ncu summary of this workload, if present."""
-    p = ROOT / "profiles" / f"gather_{workload}.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+# Bytes of per-ray state a traversal launch moves besides the tree: a closest-hit ray reads its
+# queue entry (4), origin and direction (32) and the job word of its throughput (16) and writes its
+# hit (8); an occlusion ray reads its 48-byte record and, when the light is visible, adds its term to
+# the accumulator (16 read + 16 written, counted for every ray: an upper bound).
+CLOSEST_RAY_BYTES = 4 + 32 + 16 + 8
+OCCLUSION_RAY_BYTES = 48 + 32
+TRI_BYTES = 48  # one leaf-ordered triangle record: v0 (+ index), v1 - v0, v2 - v0
+
+
+def trace_roofline(prof_ev, prof_ct, peak: float, peak_kind: str, gather_ms: float) -> dict:
+    """Roofline of wf_trace_kernel, the frame's dominant kernel (closest-hit and occlusion rays in one
+    persistent launch per iteration).  Algorithmic bytes per launch = the records its rays visit x
+    the record size + the leaf triangles they test x 48 B + the per-ray state bytes above, all
+    counted on the device by the counting variant of the kernel over one frame; the launch duration
+    is the CUDA-event time of the ordinary kernel's launches over two frames.  The records are mostly
+    served by L1 / L2 (DRAM traffic is measured by ncu: profiles/), so this is the rate at which the
+    kernel consumes tree bytes, set against the HBM peak."""
+    f_ct = max(prof_ct.frames, 1)
+    launches = prof_ev.trace_launches / max(prof_ev.frames, 1)
+    ms_launch = prof_ev.ms_trace / max(prof_ev.trace_launches, 1)
+    rb = prof_ct.record_bytes
+    rec = (prof_ct.records_closest + prof_ct.records_occlusion) / f_ct
+    tests = (prof_ct.tri_tests_closest + prof_ct.tri_tests_occlusion) / f_ct
+    per_frame = (rb * rec + TRI_BYTES * tests + CLOSEST_RAY_BYTES * prof_ct.closest_rays / f_ct
+                 + OCCLUSION_RAY_BYTES * prof_ct.occlusion_rays / f_ct)
+    per_launch = per_frame / max(launches, 1)
+    achieved = per_launch / (ms_launch / 1000.0) / 1e9
+    rays_c, rays_o = max(prof_ct.closest_rays, 1), max(prof_ct.occlusion_rays, 1)
+    return {"bound": "hbm", "kernel": "wf_trace_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s",
+            "algorithmic_bytes_per_launch": per_launch, "launch_ms": ms_launch, "launches_per_step": launches,
+            "share_of_gather": prof_ev.ms_trace / max(prof_ev.ms_gather, 1e-9),
+            "shade_share_of_gather": prof_ev.ms_shade / max(prof_ev.ms_gather, 1e-9),
+            "gather_ms": gather_ms,
+            "work": {"record_bytes": rb,
+                     "records_per_closest_ray": prof_ct.records_closest / rays_c,
+                     "records_per_occlusion_ray": prof_ct.records_occlusion / rays_o,
+                     "tri_tests_per_closest_ray": prof_ct.tri_tests_closest / rays_c,
+                     "tri_tests_per_occlusion_ray": prof_ct.tri_tests_occlusion / rays_o,
+                     "closest_rays_per_frame": prof_ct.closest_rays / f_ct,
+                     "occlusion_rays_per_frame": prof_ct.occlusion_rays / f_ct},
+            "traffic_note": "DRAM bytes per launch come from an ncu capture (profiles/), not from this run"}
 
 
 def photon_denoise_stages(steps: int, warmup: int, peak: float) -> dict:
@@ -642,6 +674,17 @@ def run_ours(args, w):
     e2e_wall, e2e_seg_all = job_totals(dist, t1 - t0, e2e_seg, device="cuda")
     e2e_value = e2e_seg_all / e2e_wall
 
+    # ---- kernel-level profile of the dominant kernel (untimed frames after the timed region) -----
+    # Two frames with CUDA events around every traversal / shade launch, then one frame of the
+    # counting traversal kernels (records visited and leaf triangle tests per kind of ray).
+    r.set_profiling(rt._abi.PROFILE_EVENTS)
+    r.render_frames(2)
+    prof_ev = r.read_profile()
+    r.set_profiling(rt._abi.PROFILE_COUNT)
+    r.render_frames(1)
+    prof_ct = r.read_profile()
+    r.set_profiling(0)
+
     if rank == 0:
         gather_ms = s1.ms_gather_sum / max(s1.timed_frames, 1)
         resolve_ms = s1.ms_resolve_sum / max(s1.timed_frames, 1)
@@ -650,17 +693,8 @@ def run_ours(args, w):
         oscene, ocfg = oracle_workload(w)
         cpu_val, cpu_desc, work = cpu_sample(oscene, ocfg, args.cpu_seconds, threads)
         del oscene
-        seg_per_frame = segments / max(args.steps, 1)
-        shd_per_frame = shadow / max(args.steps, 1)
-        rays = seg_per_frame + shd_per_frame
-        # Algorithmic bytes of one gather launch: 48 B per node fetch, 4 + 48 B per triangle test
-        # (prim index + vertices), 128 + 64 B of triangle + material per hit, 48 B of frame outputs
-        # per pixel.
-        algo = (rays * (48.0 * work["nodes_per_ray"] + 52.0 * work["tris_per_ray"])
-                + 192.0 * seg_per_frame * work["hit_fraction"] + 48.0 * cfg.width * cfg.height)
         peak, peak_kind = hbm_peak()
-        achieved = algo / (gather_ms / 1000.0) / 1e9
-        traffic = load_traffic(args.workload)
+        roofline = trace_roofline(prof_ev, prof_ct, peak, peak_kind, gather_ms)
         stages = photon_denoise_stages(args.steps, args.warmup, peak) if args.stages else None
         pool = scene_pool(32, 7) if (args.batched or args.served) else None
         batched = batched_leg(args.batched_jobs, args.batched_steps, 2, pool) if args.batched else None
@@ -675,16 +709,8 @@ def run_ours(args, w):
             "shadow_rays_per_s": shd_all / (ms_max / 1000.0),
             "gpu_launches": int(frame_launches([cfg]) * args.steps),
             "kernel_ms": {"gather": gather_ms, "resolve": resolve_ms},
-            "roofline": {"bound": "hbm", "kernel": "gather pass (wf_generate, wf_trace, wf_shade, wf_finalize)",
-                         "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         # DRAM bytes actually moved per pass / pass time: the records are mostly
-                         # served from L1 / L2, so this sits far below the algorithmic rate.
-                         "dram_achieved": traffic / (gather_ms / 1000.0) / 1e9 if traffic else None,
-                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                         else "fallback 6.8 TB/s",
-                         "algorithmic_bytes_per_launch": algo,
-                         "work_per_ray": work},
+            "roofline": roofline,
+            "oracle_work_per_ray": work,
             "cpu_baseline": {"value": cpu_val, "unit": "segments/s", "cores": threads, "kind": "port",
                              "sample": cpu_desc},
             "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": 96 + 80,

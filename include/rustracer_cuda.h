@@ -338,6 +338,29 @@ int rt_synchronize(rt_renderer *r);
 /* Waits for the renderer's stream.  Per-kernel sums cover the frames since the previous call. */
 int rt_get_stats(rt_renderer *r, rt_frame_stats *out);
 int rt_get_grid_params(const rt_renderer *r, rt_grid_params *out);
+
+/* Kernel-level profile of the gather pass (no counterpart in the reference, whose frame is one
+ * megakernel dispatch).  With RT_PROFILE_EVENTS set, every later rt_render_frame records CUDA events
+ * around each launch of the traversal, shade and photon-lookup kernels and waits for its frame; with
+ * RT_PROFILE_COUNT it runs the counting variants of the traversal kernels (same rays and results),
+ * which add the records each kind of ray visits and its leaf triangle tests.  Images are unchanged
+ * either way.  rt_read_profile returns the sums over the profiled frames since the previous read and
+ * resets them; rt_set_profiling(r, 0) stops profiling. */
+#define RT_PROFILE_EVENTS 1u
+#define RT_PROFILE_COUNT 2u
+typedef struct rt_trace_profile {
+    uint64_t frames;                 /* profiled frames summed here                               */
+    uint64_t trace_launches, shade_launches, photon_launches;
+    double ms_trace, ms_shade, ms_photon;   /* device time of those launches (RT_PROFILE_EVENTS) */
+    double ms_gather;                /* whole gather passes of the profiled frames               */
+    uint64_t closest_rays, occlusion_rays;  /* closest-hit (path segment) and occlusion rays       */
+    uint64_t records_closest, records_occlusion;      /* traversal records visited (RT_PROFILE_COUNT) */
+    uint64_t tri_tests_closest, tri_tests_occlusion;  /* leaf triangle tests (RT_PROFILE_COUNT)      */
+    uint32_t record_bytes;           /* bytes of one traversal record: 128 four-wide, 64 two-wide */
+    uint32_t pixels;                 /* pixels of one frame                                       */
+} rt_trace_profile;
+int rt_set_profiling(rt_renderer *r, uint32_t flags);
+int rt_read_profile(rt_renderer *r, rt_trace_profile *out);
 /* The renderer's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
 void *rt_renderer_stream(rt_renderer *r);
 

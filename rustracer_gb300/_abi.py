@@ -141,6 +141,20 @@ class FrameStats(C.Structure):
                 ("graph_captures", C.c_uint64)]
 
 
+class TraceProfile(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("trace_launches", C.c_uint64), ("shade_launches", C.c_uint64),
+                ("photon_launches", C.c_uint64), ("ms_trace", C.c_double), ("ms_shade", C.c_double),
+                ("ms_photon", C.c_double), ("ms_gather", C.c_double), ("closest_rays", C.c_uint64),
+                ("occlusion_rays", C.c_uint64), ("records_closest", C.c_uint64), ("records_occlusion", C.c_uint64),
+                ("tri_tests_closest", C.c_uint64), ("tri_tests_occlusion", C.c_uint64), ("record_bytes", u32),
+                ("pixels", u32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+PROFILE_EVENTS, PROFILE_COUNT = 1, 2
+
 SERVER_BATCHED, SERVER_PLAIN = 0, 1
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
@@ -203,6 +217,8 @@ _PROTOS: dict[str, tuple] = {
     "rt_sample_count": (u32, [vp]),
     "rt_synchronize": (C.c_int, [vp]),
     "rt_get_stats": (C.c_int, [vp, P(FrameStats)]),
+    "rt_set_profiling": (C.c_int, [vp, u32]),
+    "rt_read_profile": (C.c_int, [vp, P(TraceProfile)]),
     "rt_get_grid_params": (C.c_int, [vp, P(GridParams)]),
     "rt_renderer_stream": (vp, [vp]),
     "rt_read_accumulation": (C.c_int, [vp, vp, C.c_uint64]),

@@ -797,7 +797,9 @@ __device__ __forceinline__ void shadow_resolve(const WaveParams &p, uint32_t rec
 // start early and the shorter occlusion rays fill the end.
 constexpr uint32_t kNoIter = 0xFFFFFFFFu;
 
-template <int kStack, int kBlock, bool kWide>
+// kCount: the profiling variant, which also counts the records each kind of ray visits and its leaf
+// triangle tests into p.work (one atomic per warp at exit); the same rays and results otherwise.
+template <int kStack, int kBlock, bool kWide, bool kCount>
 __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
                                                           uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
@@ -814,6 +816,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
     bool has = false, occlusion = false, any_hit = false;
     uint32_t id = 0;  // path slot (closest hit) or shadow record (occlusion)
     float limit = 0.0f;
+    uint32_t work[4] = {0u, 0u, 0u, 0u};  // kCount: records closest / occlusion, tests closest / occlusion
     for (;;) {
         const uint32_t item = warp_take(feed, !has, n_ext + n_shd, fetch, chunk);
         if (item != 0xFFFFFFFFu) {
@@ -845,13 +848,28 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
         for (uint32_t k = 0; k < steps; ++k) {
-            if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl)
-                      : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl)) {
+            uint32_t tests = 0u;
+            const bool visiting = has;
+            if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)
+                      : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
                 else p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
                 has = false;
             }
+            if (kCount && visiting) {
+                work[occlusion ? 1 : 0] += 1u;
+                work[occlusion ? 3 : 2] += tests;
+            }
             if (!__any_sync(0xFFFFFFFFu, has)) break;
+        }
+    }
+    if (kCount && p.work) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            uint32_t v = work[i];
+#pragma unroll
+            for (uint32_t d = 16u; d > 0u; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+            if ((threadIdx.x & 31u) == 0u) atomicAdd(p.work + i, (unsigned long long)v);
         }
     }
 }
@@ -939,10 +957,13 @@ using ExtendKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t);
 using TraceKernel = void (*)(const WaveParams, uint32_t, uint32_t, uint32_t, uint32_t);
 
 template <int kStack, int kBlock>
-void pick(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &trc) {
+void pick(const WaveTuning &t, bool wide, bool count, ExtendKernel &ext, TraceKernel &trc) {
     if ((int)t.stack_entries == kStack && (int)t.block_threads == kBlock) {
         ext = wide ? wf_extend_kernel<kStack, kBlock, true> : wf_extend_kernel<kStack, kBlock, false>;
-        trc = wide ? wf_trace_kernel<kStack, kBlock, true> : wf_trace_kernel<kStack, kBlock, false>;
+        if (count)
+            trc = wide ? wf_trace_kernel<kStack, kBlock, true, true> : wf_trace_kernel<kStack, kBlock, false, true>;
+        else
+            trc = wide ? wf_trace_kernel<kStack, kBlock, true, false> : wf_trace_kernel<kStack, kBlock, false, false>;
     }
 }
 
@@ -951,18 +972,18 @@ size_t trav_smem_bytes(const WaveTuning &t) {
     return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves);
 }
 
-void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &shd) {
+void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &shd, bool count = false) {
     ext = nullptr;
     shd = nullptr;
-    pick<32, 64>(t, wide, ext, shd);
-    pick<32, 128>(t, wide, ext, shd);
-    pick<32, 256>(t, wide, ext, shd);
-    pick<48, 64>(t, wide, ext, shd);
-    pick<48, 128>(t, wide, ext, shd);
-    pick<48, 256>(t, wide, ext, shd);
-    pick<64, 64>(t, wide, ext, shd);
-    pick<64, 128>(t, wide, ext, shd);
-    pick<64, 256>(t, wide, ext, shd);
+    pick<32, 64>(t, wide, count, ext, shd);
+    pick<32, 128>(t, wide, count, ext, shd);
+    pick<32, 256>(t, wide, count, ext, shd);
+    pick<48, 64>(t, wide, count, ext, shd);
+    pick<48, 128>(t, wide, count, ext, shd);
+    pick<48, 256>(t, wide, count, ext, shd);
+    pick<64, 64>(t, wide, count, ext, shd);
+    pick<64, 128>(t, wide, count, ext, shd);
+    pick<64, 256>(t, wide, count, ext, shd);
 }
 
 }  // namespace
@@ -972,7 +993,10 @@ void opt_in_smem() {
     // Blocks above 48 KB of dynamic shared memory need the opt-in; set it for every shape.
     const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack});
     cudaFuncSetAttribute(wf_extend_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         bytes);
+    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         bytes);
 }
 
 template <bool kWide>
@@ -1010,7 +1034,7 @@ cudaError_t launch_extend(const WaveParams &p, uint32_t iter, uint64_t max_items
 }
 
 cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
-                             const WaveTuning &tune, cudaStream_t st) {
+                             const WaveTuning &tune, cudaStream_t st, WaveProfile *prof) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4 * (size_t)(iters + 1), st)) != cudaSuccess) return e;
     uint64_t slots = 0;
@@ -1028,7 +1052,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     normalize_tuning(t, wide ? wide_need : stack_need);
     ExtendKernel ext;
     TraceKernel trc;
-    trav_kernels(t, wide, ext, trc);
+    trav_kernels(t, wide, ext, trc, p.work != nullptr);
     const size_t smem = trav_smem_bytes(t);
     // A launch carries up to one path per slot plus one occlusion ray per slot.
     const uint64_t blocks_needed = (2u * slots + t.block_threads - 1u) / t.block_threads;
@@ -1049,12 +1073,34 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     void (*shade)(const WaveParams, uint32_t) =
         photons ? (debug ? wf_shade_kernel<true, true> : wf_shade_kernel<true, false>)
                 : (debug ? wf_shade_kernel<false, true> : wf_shade_kernel<false, false>);
+    uint32_t n_trc = 0, n_shd = 0, n_pho = 0;
+    // Events of the profiled pass around one launch (never inside a captured graph: prof is null there).
+    auto mark = [&](cudaEvent_t *ev, uint32_t i, int side) {
+        if (prof && ev) cudaEventRecord(ev[2 * i + side], st);
+    };
     for (uint32_t it = 0; it < iters; ++it) {
+        mark(prof ? prof->trace_ev : nullptr, n_trc, 0);
         trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps);
+        mark(prof ? prof->trace_ev : nullptr, n_trc++, 1);
+        mark(prof ? prof->shade_ev : nullptr, n_shd, 0);
         shade<<<shade_grid, 128, 0, st>>>(p, it);
-        if (photons) wf_photon_kernel<<<photon_grid, 128, 0, st>>>(p, it);
+        mark(prof ? prof->shade_ev : nullptr, n_shd++, 1);
+        if (photons) {
+            mark(prof ? prof->photon_ev : nullptr, n_pho, 0);
+            wf_photon_kernel<<<photon_grid, 128, 0, st>>>(p, it);
+            mark(prof ? prof->photon_ev : nullptr, n_pho++, 1);
+        }
     }
-    if (iters) trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
+    if (iters) {
+        mark(prof ? prof->trace_ev : nullptr, n_trc, 0);
+        trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
+        mark(prof ? prof->trace_ev : nullptr, n_trc++, 1);
+    }
+    if (prof) {
+        prof->trace_launches = n_trc;
+        prof->shade_launches = n_shd;
+        prof->photon_launches = n_pho;
+    }
     for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);
     wf_count_kernel<<<1, 32, 0, st>>>(p, iters);
     return cudaGetLastError();

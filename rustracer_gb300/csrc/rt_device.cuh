@@ -425,8 +425,10 @@ __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, Warp
     return found;
 }
 
+// tests_out (optional): the lane's leaf triangle tests of this step (the work counters of the
+// profiling kernels).
 __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
-                                               WarpLeaves &w) {
+                                               WarpLeaves &w, uint32_t *tests_out = nullptr) {
     bool hl = false, hr = false;
     float le = 0.0f, re = 0.0f;
     uint32_t lref = 0u, lcnt = 0u, rref = 0u, rcnt = 0u;
@@ -449,6 +451,7 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
     }
     const uint32_t nl = (hl && lcnt != 0u) ? lcnt : 0u;
     const uint32_t n = nl + ((hr && rcnt != 0u) ? rcnt : 0u);
+    if (tests_out) *tests_out = n;
     // The next record does not depend on this record's leaf results (they only lower st.t for later
     // box tests), so the lane moves on first and its next record is on the way to L1 while the warp
     // tests leaves.
@@ -490,7 +493,7 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
 // first; the stack holds every pending entry).  Same results as the two-wide walk: the closest hit
 // below the starting st.t, ties resolved to the lowest prim slot as in the two-wide walk.
 __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
-                                                WarpLeaves &w) {
+                                                WarpLeaves &w, uint32_t *tests_out = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t n = 0u;
     bool exhausted = false;
@@ -563,6 +566,7 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
         }
         if (!exhausted) asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 8ull * st.node));
     }
+    if (tests_out) *tests_out = n;
     const bool found = warp_leaf_rounds(st, n, w, [&](uint32_t o, uint32_t j) {
         const uint4 r = w.leaf_ref[o], b = w.leaf_start[o];
         const uint32_t i = (j >= b.y ? 1u : 0u) + (j >= b.z ? 1u : 0u) + (j >= b.w ? 1u : 0u);

@@ -42,6 +42,9 @@ struct WaveParams {
     float4 *shadow;    // 3 per deferred NEE ray: (origin, max_dist), (dir, slot), (contribution, tag)
     float4 *preq;      // 3 per photon-map lookup: (hit point, slot), (normal, sample), (throughput, job)
     unsigned long long *counters;  // [0] segments, [1] shadow rays (cumulative)
+    // Work counters of the profiling traversal kernels (null otherwise): traversal records visited
+    // by closest-hit / occlusion rays, then their leaf triangle tests.
+    unsigned long long *work;
 };
 // Host-side shape of a job for the per-job launches.
 struct JobShape {
@@ -62,9 +65,16 @@ struct WaveTuning {
 WaveTuning default_tuning();
 // Clamps a tuning to supported values (stack raised to `stack_need`); false if it had to change.
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need);
+// Optional instrumentation of one gather pass: CUDA events recorded before and after every launch of
+// the traversal, shade and photon-lookup kernels (2 per launch; arrays of at least 2 * (iters + 1)),
+// and the counting variants of the traversal kernels when p.work is set.
+struct WaveProfile {
+    cudaEvent_t *trace_ev, *shade_ev, *photon_ev;
+    uint32_t trace_launches, shade_launches, photon_launches;  // written by launch_wavefront
+};
 // generate (per job), iters x (extend, shade, shadow) over all jobs, finalize (per job), counters.
 cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t n_jobs, uint32_t iters, int num_sms,
-                             const WaveTuning &tune, cudaStream_t st);
+                             const WaveTuning &tune, cudaStream_t st, WaveProfile *prof = nullptr);
 int device_sm_count();
 // One-time kernel attributes (shared-memory opt-ins); call before capturing launches into a graph.
 void prepare_kernels();

@@ -62,3 +62,4 @@ static_assert(sizeof(rt_request) == 164 && offsetof(rt_request, config) == 16 &&
               "rt_request");
 static_assert(sizeof(rt_job_status) == 48, "rt_job_status");
 static_assert(sizeof(rt_server_stats) == 128, "rt_server_stats");
+static_assert(sizeof(rt_trace_profile) == 120 && offsetof(rt_trace_profile, record_bytes) == 112, "rt_trace_profile");

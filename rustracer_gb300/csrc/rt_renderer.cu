@@ -245,6 +245,8 @@ rt_renderer::~rt_renderer() {
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);
     }
+    for (cudaEvent_t e : prof_ev)
+        if (e) cudaEventDestroy(e);
     if (res) rt::resident_scene_release(res);
 }
 
@@ -555,7 +557,11 @@ extern "C" int rt_render_frame(rt_renderer *r) {
                               c.debug_view != 0u ? 1u : 0u,
                               r->scene.wnodes ? 1u : 0u,
                               r->scene.wide_stack};
-    RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
+    if (r->prof_flags) {
+        if (int st = rt::profiled_gather(r, wp, shape, iters)) return st;
+    } else {
+        RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
+    }
     RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
     if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
     float4 *result = nullptr;
@@ -567,6 +573,92 @@ extern "C" int rt_render_frame(rt_renderer *r) {
     if (fe[3]) RT_CK(cudaEventRecord(fe[3], s));
     r->frames += 1;
     r->have_frame_timing = true;
+    return RT_OK;
+}
+
+namespace rt {
+// The gather pass of a profiled frame: launches bracketed by events, the counting traversal kernels
+// when asked, then a wait for the pass and the sums added to r->prof.
+int profiled_gather(rt_renderer *r, rtd::WaveParams wp, const rtd::JobShape &shape, uint32_t iters) {
+    cudaStream_t s = r->stream;
+    const size_t per_kind = 2 * ((size_t)iters + 1);
+    const size_t need = 3 * per_kind + 2;
+    while (r->prof_ev.size() < need) {
+        cudaEvent_t e = nullptr;
+        RT_CK(cudaEventCreate(&e));
+        r->prof_ev.push_back(e);
+    }
+    const bool count = (r->prof_flags & RT_PROFILE_COUNT) != 0u;
+    if (count) {
+        if (!r->d_work.p) RT_CK(r->d_work.alloc(4 * sizeof(unsigned long long)));
+        RT_CK(cudaMemsetAsync(r->d_work.p, 0, 4 * sizeof(unsigned long long), s));
+        wp.work = r->d_work.as<unsigned long long>();
+    }
+    const bool events = (r->prof_flags & RT_PROFILE_EVENTS) != 0u;
+    cudaEvent_t *ev = r->prof_ev.data();
+    rtd::WaveProfile prof{events ? ev : nullptr, events ? ev + per_kind : nullptr, events ? ev + 2 * per_kind : nullptr,
+                          0u, 0u, 0u};
+    cudaEvent_t *pass = ev + 3 * per_kind;
+    RT_CK(cudaEventRecord(pass[0], s));
+    RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s, &prof));
+    RT_CK(cudaEventRecord(pass[1], s));
+    RT_CK(cudaStreamSynchronize(s));
+    auto span = [](cudaEvent_t a, cudaEvent_t b) {
+        float v = 0.0f;
+        return cudaEventElapsedTime(&v, a, b) == cudaSuccess ? (double)v : 0.0;
+    };
+    rt_trace_profile &p = r->prof;
+    p.frames += 1;
+    p.trace_launches += prof.trace_launches;
+    p.shade_launches += prof.shade_launches;
+    p.photon_launches += prof.photon_launches;
+    if (events) {
+        for (uint32_t i = 0; i < prof.trace_launches; ++i) p.ms_trace += span(ev[2 * i], ev[2 * i + 1]);
+        for (uint32_t i = 0; i < prof.shade_launches; ++i)
+            p.ms_shade += span(ev[per_kind + 2 * i], ev[per_kind + 2 * i + 1]);
+        for (uint32_t i = 0; i < prof.photon_launches; ++i)
+            p.ms_photon += span(ev[2 * per_kind + 2 * i], ev[2 * per_kind + 2 * i + 1]);
+    }
+    p.ms_gather += span(pass[0], pass[1]);
+    std::vector<uint32_t> counts(4 * ((size_t)iters + 1));
+    RT_CK(cudaMemcpy(counts.data(), wp.counts, counts.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < iters; ++i) {
+        p.closest_rays += counts[4 * i];
+        p.occlusion_rays += counts[4 * i + 1];
+    }
+    if (count) {
+        unsigned long long w[4];
+        RT_CK(cudaMemcpy(w, r->d_work.p, sizeof(w), cudaMemcpyDeviceToHost));
+        p.records_closest += w[0];
+        p.records_occlusion += w[1];
+        p.tri_tests_closest += w[2];
+        p.tri_tests_occlusion += w[3];
+    }
+    p.record_bytes = shape.wide ? 128u : 64u;
+    p.pixels = shape.npix;
+    return RT_OK;
+}
+}  // namespace rt
+
+extern "C" int rt_set_profiling(rt_renderer *r, uint32_t flags) {
+    if (int st = check_renderer(r, "rt_set_profiling")) return st;
+    if (flags & ~(RT_PROFILE_EVENTS | RT_PROFILE_COUNT)) {
+        set_error("rt_set_profiling: unknown flags 0x%x", flags);
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    r->prof_flags = flags;
+    return RT_OK;
+}
+
+extern "C" int rt_read_profile(rt_renderer *r, rt_trace_profile *out) {
+    if (int st = check_renderer(r, "rt_read_profile")) return st;
+    if (!out) {
+        set_error("rt_read_profile: null out");
+        return RT_ERR_INVALID_ARGUMENT;
+    }
+    RT_CK(cudaStreamSynchronize(r->stream));
+    *out = r->prof;
+    r->prof = rt_trace_profile{};
     return RT_OK;
 }
 

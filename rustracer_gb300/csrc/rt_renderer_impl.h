@@ -216,6 +216,12 @@ struct rt_renderer {
     uint32_t last_denoise_passes = 0;
     rt::Events events;
     rt::FrameEventRing ring;
+    // Gather-pass profiling (rt_set_profiling): flags, events around the profiled launches (2 per
+    // launch of each kind, plus the pass bounds), the counting kernels' work counters, the sums.
+    uint32_t prof_flags = 0;
+    std::vector<cudaEvent_t> prof_ev;
+    rt::DevBuf d_work;
+    rt_trace_profile prof{};
     ~rt_renderer();
     // Device bytes this renderer owns (its resident scene not included).
     uint64_t device_bytes() const;
@@ -244,4 +250,6 @@ int enqueue_denoise(rt_renderer *r, float alpha, const float *alpha_dev, cudaStr
 int enqueue_resolve(rt_renderer *r, const float4 *result, float alpha, const float *alpha_dev, cudaStream_t st);
 // Both, on stream `st`.
 int enqueue_post(rt_renderer *r, float alpha, const float *alpha_dev, cudaStream_t st);
+// The gather pass of a frame rendered with profiling on (rt_set_profiling); waits for it.
+int profiled_gather(rt_renderer *r, rtd::WaveParams wp, const rtd::JobShape &shape, uint32_t iters);
 }  // namespace rt

@@ -251,6 +251,16 @@ class Renderer:
         A.check("rt_get_stats", self._lib.rt_get_stats(self._h, C.byref(s)))
         return s
 
+    def set_profiling(self, flags: int) -> None:
+        """A.PROFILE_EVENTS (events around each traversal / shade / photon-lookup launch) and / or
+        A.PROFILE_COUNT (counting traversal kernels) for the following frames; 0 turns it off."""
+        A.check("rt_set_profiling", self._lib.rt_set_profiling(self._h, flags))
+
+    def read_profile(self) -> A.TraceProfile:
+        p = A.TraceProfile()
+        A.check("rt_read_profile", self._lib.rt_read_profile(self._h, C.byref(p)))
+        return p
+
     def stream(self) -> int:
         return int(self._lib.rt_renderer_stream(self._h) or 0)
 

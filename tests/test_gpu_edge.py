@@ -201,3 +201,32 @@ def test_config3_photon_grid_full_size(gpu, orc):
     o2 = oracle_for(orc, s, cfg, s.default_camera())
     o2.rebuild_photons()
     assert match_frac(ph.view(np.float32), o2.photons.view(np.float32), rtol=1e-4, atol=1e-4) >= 0.999
+
+
+def test_profiled_frames_render_the_same_image(gpu):
+    """Profiling (events around the launches, counting traversal kernels) leaves every image and
+    count as it is; its ray counts are the frame statistics' and every ray visits a record."""
+    s = rt.Scene.icosphere_room(level=4, seed=2, sigma=0.02, tex_size=32)
+    cfg = rt.RenderConfig(width=96, height=64, spp=2, accumulate_frames=3, enable_denoise=False, max_bounces=6)
+    imgs = []
+    for flags in (0, A.PROFILE_EVENTS, A.PROFILE_COUNT, A.PROFILE_EVENTS | A.PROFILE_COUNT):
+        r = rt.Renderer(s, cfg)
+        r.update_camera(s.default_camera())
+        r.set_profiling(flags)
+        r.render_frames(3)
+        imgs.append(r.read_accumulation())
+        p = r.read_profile()
+        st = r.stats()
+        r.close()
+        if not flags:
+            assert p.frames == 0
+            continue
+        assert p.frames == 3 and p.pixels == 96 * 64 and p.record_bytes == 128
+        assert p.closest_rays == st.segments and p.occlusion_rays == st.shadow_rays
+        assert p.trace_launches == 3 * (2 * 6 + 1) and p.shade_launches == 3 * 2 * 6
+        if flags & A.PROFILE_EVENTS:
+            assert 0.0 < p.ms_trace < p.ms_gather and 0.0 < p.ms_shade < p.ms_gather
+        if flags & A.PROFILE_COUNT:
+            assert p.records_closest >= p.closest_rays and p.records_occlusion >= p.occlusion_rays
+            assert p.tri_tests_closest > 0 and p.tri_tests_occlusion > 0
+    assert all(np.array_equal(imgs[0], im) for im in imgs[1:])

@@ -71,6 +71,11 @@ def test_oracle_layouts_agree(orc):
         for (name, _), (name2, _) in zip(mine._fields_, theirs._fields_):
             assert getattr(mine, name).offset == getattr(theirs, name2).offset
     assert orc.PHOTON_DTYPE.itemsize == C.sizeof(A.Photon)
+    for mine, theirs in [(A.SceneDesc, orc.SceneDesc), (A.Camera, orc.Camera), (A.TextureArray, orc.TextureArray)]:
+        assert C.sizeof(mine) == C.sizeof(theirs)
+        for (name, _), (name2, _) in zip(mine._fields_, theirs._fields_):
+            assert name == name2 and getattr(mine, name).offset == getattr(theirs, name2).offset
+    assert orc.BVH_NODE_DTYPE.itemsize == C.sizeof(A.BVHNode)
 
 
 def test_backend_struct_sizes_match_the_header():
@@ -83,6 +88,7 @@ def test_backend_struct_sizes_match_the_header():
     assert A.Request.config.offset == 16 and A.Request.camera.offset == 112
     assert C.sizeof(A.JobStatus) == 48
     assert C.sizeof(A.ServerStats) == 128
+    assert C.sizeof(A.TraceProfile) == 120 and A.TraceProfile.record_bytes.offset == 112
 
 
 def test_traversal_width_setting():
