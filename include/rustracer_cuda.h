@@ -525,11 +525,18 @@ int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_params *gp, uin
  *   - Scratch lives in one file-scope device array of RT_NOALLOC_SCRATCH_BYTES that every GPU loading
  *     the library holds until the process exits; sizes above RT_NOALLOC_MAX_SLOTS slots or
  *     RT_NOALLOC_MAX_CELLS cells are rejected with RT_ERR_INVALID_ARGUMENT.
- *   - The first call on a device looks up that array's device address with the device current; make
- *     that first call before any stream capture.
+ *   - Each call looks up that array's device address with the calling thread's current device, so the
+ *     address stays right after cudaDeviceReset.  With CUDA's lazy module loading (the default since
+ *     CUDA 12.2) the first call on a device may be what loads this library's kernels onto it, which
+ *     creates the array there: that first call can allocate and synchronise, so make it outside the
+ *     no-allocation region (a warm-up call at start-up) or set CUDA_MODULE_LOADING=EAGER; and make it
+ *     before any stream capture.  Later calls allocate nothing.
  *   - Work is enqueued on `stream` (a cudaStream_t; NULL = the default stream) and the call returns
  *     without waiting.  All calls share the one array (its counters are cleared by each call): calls
- *     whose work overlaps on the GPU race, so order them on one stream or synchronise between them. */
+ *     whose work overlaps on the GPU race, so order them on one stream or synchronise between them.
+ *   - A CUDA error left pending by earlier, unrelated work is cleared on entry.  On RT_ERR_CUDA part
+ *     of the build may already be enqueued: the contents of d_counts, d_meta and d_sorted are then
+ *     undefined. */
 #define RT_NOALLOC_MAX_SLOTS (1u << 20)
 #define RT_NOALLOC_MAX_CELLS (1u << 18)
 #define RT_NOALLOC_SCRATCH_BYTES 9438208u

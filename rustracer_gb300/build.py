@@ -3,8 +3,10 @@
 Usage: python -m rustracer_gb300.build [--force] [--verbose]
 
 nvcc cross-compiles without a GPU.  Objects go to rustracer_gb300/_build/, the shared library to
-rustracer_gb300/librustracer_cuda.so (both git-ignored).  Translation units compile in parallel and
-are rebuilt when a source or header is newer than the object.
+rustracer_gb300/librustracer_cuda.so and the same objects as a static archive to
+rustracer_gb300/librustracer_cuda.a (all git-ignored; a static link also needs the CUDA runtime:
+-lcudart_static -lstdc++ -lpthread -ldl -lrt).  Translation units compile in parallel and are rebuilt
+when a source or header is newer than the object.
 """
 from __future__ import annotations
 
@@ -21,6 +23,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "librustracer_cuda.so"
+STATIC_LIB = PKG / "librustracer_cuda.a"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: a*b+c is rounded twice, as the WGSL shaders' separate multiply and add are.
@@ -61,7 +64,10 @@ def _stale(obj: Path, src: Path, newest_header: float) -> bool:
     return t < src.stat().st_mtime or t < newest_header
 
 
-# Image-space kernels whose weights are not compared bit for bit (their tests use 1e-4): FMA on.
+# The image-space kernels (denoise, composite + tonemap) are compiled with FMA contraction: their
+# parity tests compare within 1e-5 relative (denoise) and +-1 rgba8 step (tonemap); composite stays
+# bit-exact because its mix is written with explicitly rounded products and sum (__fmul_rn /
+# __fadd_rn, which are never contracted).
 FMAD_ON = {"k_image.cu"}
 
 
@@ -103,7 +109,21 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if res.returncode != 0:
             raise RuntimeError(f"linking librustracer_cuda.so failed:\n{res.stdout}\n{res.stderr}")
         os.replace(tmp, LIB)
+    if force or todo or not STATIC_LIB.exists() or any(STATIC_LIB.stat().st_mtime < o.stat().st_mtime for o in objs):
+        tmp_a = STATIC_LIB.with_suffix(".a.tmp")
+        if tmp_a.exists():
+            tmp_a.unlink()
+        res = subprocess.run([shutil.which("ar") or "ar", "rcs", str(tmp_a), *map(str, objs)], capture_output=True,
+                             text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"archiving librustracer_cuda.a failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(tmp_a, STATIC_LIB)
     return LIB
+
+
+def cuda_lib_dir() -> Path:
+    """The CUDA toolkit's library directory (libcudart_static.a for a static link)."""
+    return _cuda_lib_dir(_nvcc())
 
 
 def main(argv: list[str] | None = None) -> int:

@@ -11,8 +11,6 @@
 // array (RT_NOALLOC_SCRATCH_BYTES, 9,438,208 bytes) until the process exits.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "rt_internal.h"
 #include "rt_kernels.h"
 
@@ -30,18 +28,16 @@ constexpr size_t kTotalOff = align256(kPartialsOff + 4 * kPartialsMax);
 constexpr size_t kScratchBytes = align256(kTotalOff + 16);
 static_assert(kScratchBytes <= RT_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the declared size");
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void *g_scratch[kMaxDevices] = {};
-
 }  // namespace
 
-// Shared by every call on a device; the host learns its device address once per device.
+// Shared by every call on a device.  In host code the name is only a handle: the array's device
+// address comes from cudaGetSymbolAddress with the device current.
 static __device__ __align__(256) unsigned char g_grid_scratch[RT_NOALLOC_SCRATCH_BYTES];
 
 extern "C" int rt_stage_photon_grid_noalloc(const rt_photon *d_photons, const rt_grid_params *gp, uint32_t *d_counts,
                                             uint32_t *d_meta, rt_photon *d_sorted, void *stream) {
     rt::clear_error();
+    (void)cudaGetLastError();  // a non-sticky error left by earlier, unrelated work is not this call's
     if (!gp || !d_counts || !d_meta || !d_sorted || (gp->photon_slots && !d_photons)) {
         set_error("rt_stage_photon_grid_noalloc: null argument");
         return RT_ERR_INVALID_ARGUMENT;
@@ -63,25 +59,19 @@ extern "C" int rt_stage_photon_grid_noalloc(const rt_photon *d_photons, const rt
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (e != cudaSuccess) {
         set_error("rt_stage_photon_grid_noalloc: no usable current device (%s)", cudaGetErrorString(e));
         return RT_ERR_CUDA;
     }
+    // The array's address on the current device, looked up on every call: a lookup allocates nothing
+    // once the module is loaded, and a fresh one stays right after cudaDeviceReset reloads it.  The
+    // first call on a device may load the module (lazy loading), which creates the array.
     void *base = nullptr;
-    {
-        // First call on a device: resolve the array's device address with that device current.
-        std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_grid_scratch);
-            if (e != cudaSuccess || !p) {
-                set_error("rt_stage_photon_grid_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                          cudaGetErrorString(e));
-                return RT_ERR_CUDA;
-            }
-            g_scratch[dev] = p;
-        }
-        base = g_scratch[dev];
+    e = cudaGetSymbolAddress(&base, g_grid_scratch);
+    if (e != cudaSuccess || !base) {
+        set_error("rt_stage_photon_grid_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
+                  cudaGetErrorString(e));
+        return RT_ERR_CUDA;
     }
     unsigned char *b = static_cast<unsigned char *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -161,3 +161,34 @@ def test_mesh_defaults(lib):
     t = s.arrays()["triangles"][0]
     assert t["n0"].tolist() == [0, 1, 0] and t["uv2"].tolist() == [0, 0]
     assert t["v1"].tolist() == [1, 0, 0]
+
+
+def test_static_library_links_a_c_program(lib, tmp_path):
+    """librustracer_cuda.a (the archive a Rust build links with cargo:rustc-link-lib=static) links
+    into a plain C program with the CUDA runtime and answers through the C ABI (no device needed)."""
+    import shutil
+    import subprocess
+
+    from rustracer_gb300 import build as b
+
+    cc = shutil.which("gcc")
+    if cc is None or not b.STATIC_LIB.exists():
+        pytest.skip("no C compiler or no static archive")
+    src = tmp_path / "main.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "rustracer_cuda.h"\n'
+        "int main(void) {\n"
+        "    rt_render_config c; rt_render_config_default(&c);\n"
+        "    rt_scene *s = 0; if (rt_scene_create_cornell555(&s) != RT_OK) return 2;\n"
+        "    rt_scene_desc d; if (rt_scene_describe(s, &d) != RT_OK) return 3;\n"
+        '    printf("%s %u %llu %d\\n", rt_version(), c.width, (unsigned long long)d.triangle_count,'
+        " rt_device_count() >= 0);\n"
+        "    rt_scene_destroy(s); return 0;\n}\n")
+    exe = tmp_path / "main"
+    cmd = [cc, str(src), "-I", str(b.INCLUDE), str(b.STATIC_LIB), "-L", str(b.cuda_lib_dir()), "-lcudart_static",
+           "-lstdc++", "-lpthread", "-ldl", "-lrt", "-lm", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split()[-3:] == ["800", "36", "1"]

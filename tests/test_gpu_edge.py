@@ -119,10 +119,9 @@ def test_accumulation_controls(gpu, orc):
     o.accum[:] = 0
     lights = [rt.area_light(10, (5.0, 5.0, 5.0), 1.0), rt.area_light(11, (5.0, 5.0, 5.0), 1.0)]
     r.update_lights(lights)
-    d = s.describe()
-    for k, l in enumerate(lights):  # the same bytes into the oracle's light array
+    for k, l in enumerate(lights):  # the same bytes into the oracle's own light array
         C = __import__("ctypes")
-        C.memmove(C.addressof(d.lights.contents) + k * 64, C.addressof(l), 64)
+        C.memmove(o.desc.lights + k * 64, C.addressof(l), 64)
     cfg2 = r.config
     cfg2.spp = 2
     cfg2.exposure = 1.7

@@ -62,6 +62,18 @@ def test_noalloc_grid_matches_allocating_entry_point_on_two_calls(gpu):
         assert binned > 0
         assert np.array_equal(d_sorted.cpu().numpy()[: binned * 64], ref_sorted.view(np.uint8).ravel()[: binned * 64])
 
+    # Once the library is loaded on the device, a call takes no device memory: free memory is the same
+    # before and after a third call on the buffers above.
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    st = lib.rt_stage_photon_grid_noalloc(C.c_void_p(d_ph.data_ptr()), C.byref(g), C.c_void_p(d_counts.data_ptr()),
+                                          C.c_void_p(d_meta.data_ptr()), C.c_void_p(d_sorted.data_ptr()),
+                                          C.c_void_p(stream.cuda_stream))
+    assert st == A.RT_OK, lib.rt_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(d_counts.cpu().numpy().view(np.uint32), ref_counts)
+
     # Sizes beyond the fixed scratch are refused with a clear error, before any work is enqueued.
     g = A.GridParams.from_buffer_copy(gp)
     g.photon_slots = A.NOALLOC_MAX_SLOTS + 1
