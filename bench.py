@@ -558,7 +558,7 @@ def served_arm(mode: str, trace, pool, seconds: float, tuning: dict | None) -> d
                     tuning=tuning)
     for i, (_, sc) in enumerate(pool):
         srv.add_scene(i, sc)
-    ids = []
+    ids, t_sub = [], []
     s0 = srv.stats()
     start = time.perf_counter()
     for t_arr, spec, budget in trace:
@@ -566,6 +566,7 @@ def served_arm(mode: str, trace, pool, seconds: float, tuning: dict | None) -> d
         if delay > 0:
             time.sleep(delay)
         _, cfg, cam = job_objects(spec, pool)
+        t_sub.append(time.perf_counter() - start)
         ids.append(srv.submit(spec["scene"], cfg, cam, budget))
     rest = start + seconds - time.perf_counter()
     if rest > 0:
@@ -577,11 +578,32 @@ def served_arm(mode: str, trace, pool, seconds: float, tuning: dict | None) -> d
     ttff = [s.t_first_frame_ms - s.t_submit_ms for s in stats if s.t_first_frame_ms >= 0]
     ttb = [s.t_done_ms - s.t_submit_ms for s in stats if s.state == rt._abi.JOB_DONE]
     pct = lambda v, q: float(np.percentile(v, q)) if v else None  # noqa
+    # Over every submitted job: a job without a first frame (or not done) when the window closed is
+    # censored.  "all_jobs" counts it as +inf (a percentile that lands on one is reported as null);
+    # "all_jobs_lower_bound" counts it at its age when the window closed (a lower bound on its time).
+    ages = [1000.0 * (wall - t) for t in t_sub]
+    ttff_all = [s.t_first_frame_ms - s.t_submit_ms if s.t_first_frame_ms >= 0 else math.inf for s in stats]
+    ttb_all = [s.t_done_ms - s.t_submit_ms if s.state == rt._abi.JOB_DONE else math.inf for s in stats]
+
+    def pcts(v):
+        if not v:
+            return {"p50": None, "p95": None, "p99": None}
+        out = {}
+        for q in (50, 95, 99):
+            x = float(np.percentile(np.asarray(v, np.float64), q, method="inverted_cdf"))
+            out[f"p{q}"] = x if math.isfinite(x) else None
+        return out
+
+    censored = lambda v: [x if math.isfinite(x) else a for x, a in zip(v, ages)]  # noqa: E731
     return {
         "segments_per_s": (st.segments - s0.segments) / wall,
         "jobs_submitted": len(ids), "jobs_done": len(ttb), "jobs_started": len(ttff),
+        "unstarted_at_window_end": len(ids) - len(ttff), "unfinished_at_window_end": len(ids) - len(ttb),
         "ttff_ms": {"p50": pct(ttff, 50), "p95": pct(ttff, 95), "p99": pct(ttff, 99)},
         "time_to_budget_ms": {"p50": pct(ttb, 50), "p95": pct(ttb, 95), "p99": pct(ttb, 99)},
+        "ttff_ms_all_jobs": pcts(ttff_all), "ttff_ms_all_jobs_lower_bound": pcts(censored(ttff_all)),
+        "time_to_budget_ms_all_jobs": pcts(ttb_all),
+        "time_to_budget_ms_all_jobs_lower_bound": pcts(censored(ttb_all)),
         "job_frames": int(st.job_frames), "batch_frames": int(st.batch_frames), "max_active": int(st.max_active),
         "scene_uploads": int(st.scene_uploads), "scene_evictions": int(st.scene_evictions),
         "graph_captures": int(st.graph_captures), "peak_device_bytes": int(st.peak_bytes),
@@ -590,16 +612,19 @@ def served_arm(mode: str, trace, pool, seconds: float, tuning: dict | None) -> d
 
 def served_leg(rate: float, seconds: float, pool, tuning: dict | None, seed: int = 5) -> dict:
     """The request loop under Poisson arrivals, continuous batching against the one-job-at-a-time
-    loop on the same arrival trace.  Percentiles are over the jobs that reached their first frame /
-    their budget inside the window (the rest are still queued when it closes)."""
+    loop on the same arrival trace.  "ttff_ms" / "time_to_budget_ms" are over the jobs that reached
+    their first frame / their budget inside the window; the "all_jobs" forms cover every submitted job
+    with the ones still waiting when the window closed counted as censored (see served_arm)."""
     trace = served_trace(rate, seconds, pool, seed)
     batched = served_arm("batched", trace, pool, seconds, tuning)
     plain = served_arm("plain", trace, pool, seconds, None)
     return {
         "workload": f"Poisson arrivals at {rate} jobs/s for {seconds} s over a pool of {len(pool)} scenes "
                     f"(10k-2M triangles), budgets log-uniform in [8, 256] frames, HBM cap 120 GiB",
+        "rate_jobs_per_s": rate, "seconds": seconds,
         "batched": batched, "plain": plain,
         "speedup": batched["segments_per_s"] / max(plain["segments_per_s"], 1e-9),
+        "jobs_done_ratio": batched["jobs_done"] / max(plain["jobs_done"], 1),
     }
 
 
@@ -699,7 +724,14 @@ def run_ours(args, w):
         pool = scene_pool(32, 7) if (args.batched or args.served) else None
         batched = batched_leg(args.batched_jobs, args.batched_steps, 2, pool) if args.batched else None
         shape = batched["autotune"]["chosen"] if batched else None
-        served = served_leg(args.served_rate, args.served_seconds, pool, shape) if args.served else None
+        served = None
+        if args.served:
+            # the main rate first (its figures stay at the top level), then the others: one below the
+            # GPU's capacity (service times) and one far above it (queueing)
+            rates = [args.served_rate] + [x for x in args.served_other_rates if x != args.served_rate]
+            legs = [served_leg(x, args.served_seconds, pool, shape) for x in rates]
+            served = dict(legs[0])
+            served["by_rate"] = [{k: v for k, v in leg.items() if k != "workload"} for leg in legs]
         line = {
             "metric": "segments/s", "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -744,7 +776,9 @@ def main(argv=None) -> int:
     ap.add_argument("--batched-steps", type=int, default=3)
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the request-loop leg")
     ap.add_argument("--served-rate", type=float, default=10.0, help="Poisson arrival rate, jobs/s")
-    ap.add_argument("--served-seconds", type=float, default=20.0, help="arrival window (s)")
+    ap.add_argument("--served-seconds", type=float, default=20.0, help="arrival window (s) of each rate")
+    ap.add_argument("--served-other-rates", type=lambda x: [float(v) for v in x.split(",") if v], default=[1.0, 50.0],
+                    help="further arrival rates of the request-loop leg (comma-separated; empty for none)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]

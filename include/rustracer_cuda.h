@@ -645,6 +645,13 @@ uint32_t rt_get_traversal_width(void);
  * `image` crates, rustracer-core/src/loader.rs:36-100): h rows of 1 + stride bytes (filter type
  * first) in, h * stride unfiltered bytes out; bpp = bytes per pixel. */
 int rt_png_unfilter(const uint8_t *rows, uint32_t h, uint32_t stride, uint32_t bpp, uint8_t *out);
+/* JPEG decoding for the glTF ingest (the reference's `image` crate through gltf::import,
+ * rustracer-core/src/loader.rs:36-113, 266): baseline / extended sequential and progressive Huffman
+ * streams, 8-bit, grey or YCbCr (JFIF), sampling factors 1..2, restart intervals.  *w / *h receive the
+ * size; out_rgba (w * h * 4 bytes, alpha 255) is written when out_bytes is large enough, so a first
+ * call with out_rgba = NULL asks for the size.  RT_ERR_INVALID_ARGUMENT for any other stream. */
+int rt_jpeg_decode(const uint8_t *data, uint64_t n, uint8_t *out_rgba, uint64_t out_bytes, uint32_t *w,
+                   uint32_t *h);
 
 #ifdef __cplusplus
 } /* extern "C" */

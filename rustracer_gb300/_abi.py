@@ -248,6 +248,7 @@ _PROTOS: dict[str, tuple] = {
     "rt_scene_bvh_builder_used": (u32, [vp]),
     "rt_bvh_build_gpu": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float), u64, P(vp), P(u32)]),
     "rt_png_unfilter": (C.c_int, [P(C.c_uint8), u32, u32, u32, P(C.c_uint8)]),
+    "rt_jpeg_decode": (C.c_int, [vp, C.c_uint64, vp, C.c_uint64, P(u32), P(u32)]),
     "rt_batch_create": (C.c_int, [P(vp), u32, u32, P(vp)]),
     "rt_batch_destroy": (None, [vp]),
     "rt_batch_render_frame": (C.c_int, [vp]),

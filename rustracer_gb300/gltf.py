@@ -14,9 +14,10 @@ alpha cut-out and BLEND solid glass; textures go into one array per role (albedo
 emissive, normal), sRGB-decoded for albedo and emissive, normal maps with their scale baked into X/Y,
 sized by the first texture used in the role (others are dropped, at most 240 layers); every triangle
 of an emitting material whose emissive colour at its centroid is bright enough becomes an area light,
-and a procedural sky is added when no environment light exists.  Images are decoded by this module:
-PNG (8/16-bit grey, grey+alpha, RGB, RGBA, palette; non-interlaced); other formats fall back to the
-reference's solid grey texture, as an undecodable image does there.
+and a procedural sky is added when no environment light exists.  Images decoded here: PNG (8/16-bit
+grey, grey+alpha, RGB, RGBA, palette; non-interlaced) and JPEG (baseline, extended and progressive
+Huffman, 8-bit grey or YCbCr, through rt_jpeg_decode); other streams fall back to the reference's
+solid grey texture, as an undecodable image does there.
 """
 from __future__ import annotations
 
@@ -57,6 +58,28 @@ class Texture:
     @staticmethod
     def solid(color) -> "Texture":
         return Texture(1, 1, np.asarray(color, np.float32).reshape(1, 1, 4).copy())
+
+
+def decode_jpeg(data: bytes) -> Texture | None:
+    """JPEG to linear [0, 1] RGBA floats through the native decoder (rt_jpeg_decode); None when the
+    stream is not a JPEG this decoder handles."""
+    if data[:2] != b"\xff\xd8":
+        return None
+    lib = A.load()
+    buf = np.frombuffer(data, np.uint8)
+    w, h = A.C.c_uint32(), A.C.c_uint32()
+    if lib.rt_jpeg_decode(buf.ctypes.data, len(buf), None, 0, A.C.byref(w), A.C.byref(h)) != A.RT_OK:
+        return None
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    if lib.rt_jpeg_decode(buf.ctypes.data, len(buf), out.ctypes.data, out.nbytes, A.C.byref(w),
+                          A.C.byref(h)) != A.RT_OK:
+        return None
+    return Texture(w.value, h.value, out.astype(np.float32) / 255.0)
+
+
+def decode_image(data: bytes) -> Texture | None:
+    """The image formats the ingest decodes: PNG and JPEG."""
+    return decode_png(data) if data[:8] == b"\x89PNG\r\n\x1a\n" else decode_jpeg(data)
 
 
 def decode_png(data: bytes) -> Texture | None:
@@ -411,11 +434,11 @@ def load_gltf_model(path) -> Model:
         src = t.get("source")
         if src is not None:
             try:
-                tex = decode_png(doc.image_bytes(j["images"][src]))
+                tex = decode_image(doc.image_bytes(j["images"][src]))
             except Exception:  # noqa: BLE001 - an undecodable image becomes the solid fallback
                 tex = None
         if tex is None:
-            warnings.warn(f"texture {len(master)}: image not decodable here (PNG only); using solid grey")
+            warnings.warn(f"texture {len(master)}: image not decodable here (PNG and JPEG only); using solid grey")
             tex = Texture.solid([0.5, 0.5, 0.5, 1.0])
         master.append(tex)
     # materials
