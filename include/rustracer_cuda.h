@@ -397,7 +397,8 @@ typedef struct rt_batch rt_batch;
  * Default: 128 threads, 8 blocks per SM, chunk 32, 4 steps, 32 entries. */
 typedef struct rt_wavefront_tuning {
     uint32_t block_threads, blocks_per_sm, chunk, steps, stack_entries;
-    uint32_t _pad[3];
+    uint32_t treelet;  /* 1: the top records of the four-wide tree are staged in shared memory */
+    uint32_t _pad[2];
 } rt_wavefront_tuning;
 int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out);
 void rt_batch_destroy(rt_batch *b);

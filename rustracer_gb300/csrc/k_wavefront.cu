@@ -799,12 +799,25 @@ constexpr uint32_t kNoIter = 0xFFFFFFFFu;
 
 // kCount: the profiling variant, which also counts the records each kind of ray visits and its leaf
 // triangle tests into p.work (one atomic per warp at exit); the same rays and results otherwise.
-template <int kStack, int kBlock, bool kWide, bool kCount>
+// kTree (four-wide only): the block first stages the top kTree records of job 0's tree in shared
+// memory (after the stacks and the WarpLeaves), and lanes on that scene read them from there.
+template <int kStack, int kBlock, bool kWide, bool kCount, int kTree>
 __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const __grid_constant__ WaveParams p, uint32_t ext_iter,
                                                           uint32_t shd_iter, uint32_t chunk, uint32_t steps) {
     extern __shared__ uint32_t stack_smem[];
     uint32_t *stk = stack_smem + threadIdx.x;
     WarpLeaves &wl = reinterpret_cast<WarpLeaves *>(stack_smem + kStack * kBlock)[threadIdx.x >> 5];
+    float4 *tree = nullptr;
+    const float4 *tree_src = nullptr;
+    uint32_t tree_n = 0u;
+    if (kTree > 0) {
+        tree = reinterpret_cast<float4 *>(reinterpret_cast<WarpLeaves *>(stack_smem + kStack * kBlock) + kBlock / 32);
+        const DevScene &s0 = p.jobs[0].scene;
+        tree_src = s0.wnodes;
+        tree_n = s0.wnode_count < (uint32_t)kTree ? s0.wnode_count : (uint32_t)kTree;
+        for (uint32_t i = threadIdx.x; i < 8u * tree_n; i += kBlock) tree[i] = __ldg(tree_src + i);
+        __syncthreads();
+    }
     const uint32_t n_ext = ext_iter != kNoIter ? p.counts[4 * ext_iter] : 0u;
     const uint32_t n_shd = shd_iter != kNoIter ? p.counts[4 * shd_iter + 1] : 0u;
     const uint32_t *q = p.queue[ext_iter & 1u];
@@ -850,7 +863,8 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
         for (uint32_t k = 0; k < steps; ++k) {
             uint32_t tests = 0u;
             const bool visiting = has;
-            if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)
+            if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr,
+                                        kTree > 0 ? tree : nullptr, tree_src, tree_n)
                       : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
                 else p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
@@ -937,7 +951,7 @@ __global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t i
 // ------------------------------------------------------------------------------------------------
 // Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
-WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u}; }
+WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u, 0u}; }
 
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     const WaveTuning in = t;
@@ -948,6 +962,7 @@ bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     t.steps = t.steps < 1u ? 1u : (t.steps > 64u ? 64u : t.steps);
     const uint32_t need = stack_need > t.stack_entries ? stack_need : t.stack_entries;
     t.stack_entries = need <= 32u ? 32u : (need <= 48u ? 48u : 64u);
+    t.treelet = t.treelet ? kTreeletRecords : 0u;
     return std::memcmp(&in, &t, sizeof(t)) == 0;
 }
 
@@ -960,16 +975,22 @@ template <int kStack, int kBlock>
 void pick(const WaveTuning &t, bool wide, bool count, ExtendKernel &ext, TraceKernel &trc) {
     if ((int)t.stack_entries == kStack && (int)t.block_threads == kBlock) {
         ext = wide ? wf_extend_kernel<kStack, kBlock, true> : wf_extend_kernel<kStack, kBlock, false>;
-        if (count)
-            trc = wide ? wf_trace_kernel<kStack, kBlock, true, true> : wf_trace_kernel<kStack, kBlock, false, true>;
+        constexpr int kT = (int)kTreeletRecords;
+        const bool tree = wide && t.treelet != 0u;
+        if (!wide)
+            trc = count ? wf_trace_kernel<kStack, kBlock, false, true, 0> : wf_trace_kernel<kStack, kBlock, false, false, 0>;
+        else if (tree)
+            trc = count ? wf_trace_kernel<kStack, kBlock, true, true, kT> : wf_trace_kernel<kStack, kBlock, true, false, kT>;
         else
-            trc = wide ? wf_trace_kernel<kStack, kBlock, true, false> : wf_trace_kernel<kStack, kBlock, false, false>;
+            trc = count ? wf_trace_kernel<kStack, kBlock, true, true, 0> : wf_trace_kernel<kStack, kBlock, true, false, 0>;
     }
 }
 
-// Dynamic shared memory of a traversal block: the lane-interleaved stacks, then one WarpLeaves per warp.
-size_t trav_smem_bytes(const WaveTuning &t) {
-    return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves);
+// Dynamic shared memory of a traversal block: the lane-interleaved stacks, then one WarpLeaves per warp,
+// then the treelet (four-wide launches with t.treelet set).
+size_t trav_smem_bytes(const WaveTuning &t, bool wide = false) {
+    return (size_t)t.stack_entries * t.block_threads * sizeof(uint32_t) + (t.block_threads / 32u) * sizeof(WarpLeaves) +
+           (wide && t.treelet ? (size_t)kTreeletRecords * 8u * sizeof(float4) : 0u);
 }
 
 void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel &shd, bool count = false) {
@@ -991,12 +1012,20 @@ void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel
 template <int kStack, int kBlock, bool kWide>
 void opt_in_smem() {
     // Blocks above 48 KB of dynamic shared memory need the opt-in; set it for every shape.
-    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack});
+    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 0u});
+    const int tree_bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 1u}, true);
+    constexpr int kT = (int)kTreeletRecords;
     cudaFuncSetAttribute(wf_extend_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          bytes);
-    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          bytes);
+    if (kWide) {
+        cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, true, false, kT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes);
+        cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, true, true, kT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes);
+    }
 }
 
 template <bool kWide>
@@ -1053,7 +1082,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     ExtendKernel ext;
     TraceKernel trc;
     trav_kernels(t, wide, ext, trc, p.work != nullptr);
-    const size_t smem = trav_smem_bytes(t);
+    const size_t smem = trav_smem_bytes(t, wide);
     // A launch carries up to one path per slot plus one occlusion ray per slot.
     const uint64_t blocks_needed = (2u * slots + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;

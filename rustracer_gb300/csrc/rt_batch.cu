@@ -295,6 +295,7 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
     const uint32_t stacks[] = {32u, 48u, 64u};
     const uint32_t chunks[] = {32u, 64u, 128u, 256u};
     const uint32_t steps[] = {4u, 8u, 16u, 32u};
+    const uint32_t treelets[] = {0u, rtd::kTreeletRecords};
     auto sweep = [&](uint32_t rtd::WaveTuning::*field, const uint32_t *vals, size_t nv) {
         for (size_t i = 0; i < nv && st == RT_OK; ++i) {
             rtd::WaveTuning t = best;
@@ -313,6 +314,7 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
     sweep(&rtd::WaveTuning::stack_entries, stacks, 3);
     sweep(&rtd::WaveTuning::chunk, chunks, 4);
     sweep(&rtd::WaveTuning::steps, steps, 4);
+    sweep(&rtd::WaveTuning::treelet, treelets, 2);
     tuning = best;
     graph_mode = saved_mode;
 
@@ -340,7 +342,8 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
 namespace {
 
 rtd::WaveTuning from_c(const rt_wavefront_tuning &t) {
-    return rtd::WaveTuning{t.block_threads, t.blocks_per_sm, t.chunk, t.steps, t.stack_entries};
+    return rtd::WaveTuning{t.block_threads, t.blocks_per_sm, t.chunk, t.steps, t.stack_entries,
+                           t.treelet ? rtd::kTreeletRecords : 0u};
 }
 
 void to_c(const rtd::WaveTuning &t, rt_wavefront_tuning *out) {
@@ -350,6 +353,7 @@ void to_c(const rtd::WaveTuning &t, rt_wavefront_tuning *out) {
     out->chunk = t.chunk;
     out->steps = t.steps;
     out->stack_entries = t.stack_entries;
+    out->treelet = t.treelet ? 1u : 0u;
 }
 
 }  // namespace

@@ -492,16 +492,28 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
 // rounds, and visits the hit internal children nearest entry first (the others pushed, farthest
 // first; the stack holds every pending entry).  Same results as the two-wide walk: the closest hit
 // below the starting st.t, ties resolved to the lowest prim slot as in the two-wide walk.
+//
+// tree (optional): the block's treelet, the first tree_n records of the four-wide layout of the scene
+// whose records start at tree_src, staged in shared memory; a lane on that scene reads those records
+// from there (the breadth-first layout puts the top levels first).
 __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool any, uint32_t *stk, uint32_t stride,
-                                                WarpLeaves &w, uint32_t *tests_out = nullptr) {
+                                                WarpLeaves &w, uint32_t *tests_out = nullptr,
+                                                const float4 *tree = nullptr, const float4 *tree_src = nullptr,
+                                                uint32_t tree_n = 0u) {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t n = 0u;
     bool exhausted = false;
     if (active) {
-        const float4 *np = st.cnodes + 8ull * st.node;
         float4 q[8];
+        if (tree != nullptr && st.cnodes == tree_src && st.node < tree_n) {
+            const float4 *tp = tree + 8u * st.node;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) q[i] = __ldg(np + i);
+            for (int i = 0; i < 8; ++i) q[i] = tp[i];
+        } else {
+            const float4 *np = st.cnodes + 8ull * st.node;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) q[i] = __ldg(np + i);
+        }
         const f3 ro = st.ro, inv = st.inv;
         float key[4];
         uint32_t ref[4];
@@ -564,7 +576,8 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
             st.sp -= 1u;
             st.node = stk[st.sp * stride];
         }
-        if (!exhausted) asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 8ull * st.node));
+        if (!exhausted && !(tree != nullptr && st.cnodes == tree_src && st.node < tree_n))
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(st.cnodes + 8ull * st.node));
     }
     if (tests_out) *tests_out = n;
     const bool found = warp_leaf_rounds(st, n, w, [&](uint32_t o, uint32_t j) {

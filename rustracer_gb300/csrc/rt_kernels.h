@@ -61,7 +61,12 @@ struct WaveTuning {
     uint32_t chunk;          // queue items a warp takes per atomic: its segment of the queue
     uint32_t steps;          // traversal records between lane refills
     uint32_t stack_entries;  // shared-memory stack per lane: 32, 48 or 64 (raised to the jobs' need)
+    uint32_t treelet;        // four-wide records at the top of the tree staged in shared memory per
+                             // block: 0 or kTreeletRecords
 };
+// Records of the treelet: the first records of the breadth-first four-wide layout (the root, its
+// children and most of their children), 2 KB, which fits beside 8 blocks of 128 traversal threads.
+constexpr uint32_t kTreeletRecords = 16;
 WaveTuning default_tuning();
 // Clamps a tuning to supported values (stack raised to `stack_need`); false if it had to change.
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need);

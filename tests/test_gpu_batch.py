@@ -163,7 +163,9 @@ def test_autotune_leaves_images_unchanged(gpu, specs, alone):
 
 
 @pytest.mark.parametrize("shape", [dict(block_threads=64, blocks_per_sm=16, chunk=32, steps=4, stack_entries=48),
-                                   dict(block_threads=256, blocks_per_sm=4, chunk=256, steps=32, stack_entries=64)])
+                                   dict(block_threads=256, blocks_per_sm=4, chunk=256, steps=32, stack_entries=64),
+                                   dict(block_threads=128, blocks_per_sm=8, chunk=32, steps=4, stack_entries=32,
+                                        treelet=1)])
 def test_launch_shape_does_not_change_images(gpu, specs, alone, shape):
     rs = [make(sp) for sp in specs]
     for r in rs:
@@ -172,3 +174,18 @@ def test_launch_shape_does_not_change_images(gpu, specs, alone, shape):
         r.render_frames(5)
     for j, r in enumerate(rs):
         assert same(outputs(r), alone[j][0]), f"job {j}"
+
+
+def test_treelet_in_a_batch_of_several_scenes(gpu, specs, alone):
+    """With the treelet on, a batch stages job 0's top records; lanes on the other jobs' scenes read
+    their records from global memory.  Every job's image is its image rendered alone."""
+    rs = [make(sp) for sp in specs]
+    b = rt.Batch(rs, use_graphs=True)
+    t = dict(b.tuning)
+    t["treelet"] = 1
+    b.tuning = t
+    assert b.tuning["treelet"] == 1
+    b.render_frames(5)
+    for j, r in enumerate(rs):
+        assert same(outputs(r), alone[j][0]), f"job {j}"
+    b.close()
