@@ -46,6 +46,24 @@ __device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {fminf(a.x, b.x), fminf(
 __device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 __device__ __forceinline__ float max3(f3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
+// Three-input min / max (PTX min.f32 / max.f32 with three sources): the same value as two nested
+// fminf / fmaxf, NaN operands ignored alike.
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+// One 32-byte read-only load (ld.global.nc.v8.f32; the address is 32-byte aligned).
+__device__ __forceinline__ void ldg32(const float4 *p, float4 &a, float4 &b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
 __device__ __forceinline__ f3 mix3(f3 a, f3 b, float t) { return a * (1.0f - t) + b * t; }
 __device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
     float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
@@ -438,10 +456,10 @@ __device__ __forceinline__ bool trav_step_warp(TravState &st, bool active, bool 
         const f3 ro = st.ro, inv = st.inv;
         const f3 a0 = (xyz(q0) - ro) * inv, a1 = (xyz(q1) - ro) * inv;
         const f3 b0 = (xyz(q2) - ro) * inv, b1 = (xyz(q3) - ro) * inv;
-        le = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
-        const float lx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
-        re = fmaxf(fmaxf(fminf(b0.x, b1.x), fminf(b0.y, b1.y)), fminf(b0.z, b1.z));
-        const float rx = fminf(fminf(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y)), fmaxf(b0.z, b1.z));
+        le = fmax3f(fminf(a0.x, a1.x), fminf(a0.y, a1.y), fminf(a0.z, a1.z));
+        const float lx = fmin3f(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y), fmaxf(a0.z, a1.z));
+        re = fmax3f(fminf(b0.x, b1.x), fminf(b0.y, b1.y), fminf(b0.z, b1.z));
+        const float rx = fmin3f(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y), fmaxf(b0.z, b1.z));
         hl = le <= lx && lx > 0.0f && le < st.t;
         hr = re <= rx && rx > 0.0f && re < st.t;
         lref = __float_as_uint(q0.w);
@@ -510,9 +528,10 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
 #pragma unroll
             for (int i = 0; i < 8; ++i) q[i] = tp[i];
         } else {
+            // the 128-byte record as four 32-byte loads (records are 128-byte aligned)
             const float4 *np = st.cnodes + 8ull * st.node;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) q[i] = __ldg(np + i);
+            for (int i = 0; i < 4; ++i) ldg32(np + 2 * i, q[2 * i], q[2 * i + 1]);
         }
         const f3 ro = st.ro, inv = st.inv;
         float key[4];
@@ -522,8 +541,8 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const f3 a0 = (xyz(q[2 * c]) - ro) * inv, a1 = (xyz(q[2 * c + 1]) - ro) * inv;
-            const float te = fmaxf(fmaxf(fminf(a0.x, a1.x), fminf(a0.y, a1.y)), fminf(a0.z, a1.z));
-            const float tx = fminf(fminf(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y)), fmaxf(a0.z, a1.z));
+            const float te = fmax3f(fminf(a0.x, a1.x), fminf(a0.y, a1.y), fminf(a0.z, a1.z));
+            const float tx = fmin3f(fmaxf(a0.x, a1.x), fmaxf(a0.y, a1.y), fmaxf(a0.z, a1.z));
             const uint32_t cref = __float_as_uint(q[2 * c].w), cnt = __float_as_uint(q[2 * c + 1].w);
             const bool hit = cnt != 0xFFFFFFFFu && te <= tx && tx > 0.0f && te < st.t;
             ref[c] = cref;
