@@ -360,8 +360,12 @@ __device__ __forceinline__ uint32_t shade_key(const WaveParams &p, const uint32_
     return kind == 2u ? 1u : (kind == 1u ? 3u : 2u);
 }
 
-template <bool kPhotons, bool kDebug>
-__global__ void __launch_bounds__(128) wf_shade_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
+// kBlocks: resident blocks per SM the register allocation aims at (4: ~123 registers; 5: 96
+// registers with 62 bytes of spills; 6: 80 registers, ~200 bytes of spills, the default: the extra
+// warps hide the kernel's dependent loads, config-2 shade 7.04 -> 6.56 -> 6.41 ms per frame), chosen
+// per launch by the tuning's shade_blocks.
+template <bool kPhotons, bool kDebug, int kBlocks>
+__global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_constant__ WaveParams p, uint32_t iter) {
     __shared__ uint32_t s_count[4][kShadeKeys];  // entries per warp and key
     __shared__ uint32_t s_order[128];
     __shared__ uint8_t s_emit[128];   // by original position: 1 survives, 2 shadow ray, 4 photon lookup
@@ -951,7 +955,7 @@ __global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t i
 // ------------------------------------------------------------------------------------------------
 // Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
-WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u, 0u}; }
+WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u, 0u, 6u}; }
 
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     const WaveTuning in = t;
@@ -963,6 +967,7 @@ bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     const uint32_t need = stack_need > t.stack_entries ? stack_need : t.stack_entries;
     t.stack_entries = need <= 32u ? 32u : (need <= 48u ? 48u : 64u);
     t.treelet = t.treelet ? kTreeletRecords : 0u;
+    t.shade_blocks = t.shade_blocks >= 4u && t.shade_blocks <= 6u ? t.shade_blocks : 6u;
     return std::memcmp(&in, &t, sizeof(t)) == 0;
 }
 
@@ -1012,8 +1017,9 @@ void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel
 template <int kStack, int kBlock, bool kWide>
 void opt_in_smem() {
     // Blocks above 48 KB of dynamic shared memory need the opt-in; set it for every shape.
-    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 0u});
-    const int tree_bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 1u}, true);
+    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 0u, 4u});
+    const int tree_bytes =
+        (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 1u, 4u}, true);
     constexpr int kT = (int)kTreeletRecords;
     cudaFuncSetAttribute(wf_extend_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1087,7 +1093,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     const uint64_t blocks_needed = (2u * slots + t.block_threads - 1u) / t.block_threads;
     const uint64_t persistent = (uint64_t)num_sms * t.blocks_per_sm;
     const uint32_t grid = (uint32_t)(blocks_needed < persistent ? blocks_needed : persistent);
-    const uint64_t shade_needed = (slots + 127u) / 128u, shade_cap = (uint64_t)num_sms * 8u;
+    const uint64_t shade_needed = (slots + 127u) / 128u, shade_cap = (uint64_t)num_sms * 2u * t.shade_blocks;
     const uint32_t shade_grid = (uint32_t)(shade_needed < shade_cap ? shade_needed : shade_cap);
     const uint64_t photon_cap = (uint64_t)num_sms * 16u;
     const uint32_t photon_grid = (uint32_t)(shade_needed < photon_cap ? shade_needed : photon_cap);
@@ -1099,9 +1105,16 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
         photons = photons || jobs[j].photons != 0u;
         debug = debug || jobs[j].debug != 0u;
     }
-    void (*shade)(const WaveParams, uint32_t) =
-        photons ? (debug ? wf_shade_kernel<true, true> : wf_shade_kernel<true, false>)
-                : (debug ? wf_shade_kernel<false, true> : wf_shade_kernel<false, false>);
+    void (*shade)(const WaveParams, uint32_t);
+    if (t.shade_blocks == 6u)
+        shade = photons ? (debug ? wf_shade_kernel<true, true, 6> : wf_shade_kernel<true, false, 6>)
+                        : (debug ? wf_shade_kernel<false, true, 6> : wf_shade_kernel<false, false, 6>);
+    else if (t.shade_blocks == 5u)
+        shade = photons ? (debug ? wf_shade_kernel<true, true, 5> : wf_shade_kernel<true, false, 5>)
+                        : (debug ? wf_shade_kernel<false, true, 5> : wf_shade_kernel<false, false, 5>);
+    else
+        shade = photons ? (debug ? wf_shade_kernel<true, true, 4> : wf_shade_kernel<true, false, 4>)
+                        : (debug ? wf_shade_kernel<false, true, 4> : wf_shade_kernel<false, false, 4>);
     uint32_t n_trc = 0, n_shd = 0, n_pho = 0;
     // Events of the profiled pass around one launch (never inside a captured graph: prof is null there).
     auto mark = [&](cudaEvent_t *ev, uint32_t i, int side) {

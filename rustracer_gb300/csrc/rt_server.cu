@@ -415,8 +415,9 @@ extern "C" int rt_server_create(const rt_server_config *cfg, rt_server **out) {
     int st = s->eng.init(s->cfg.max_jobs, gm);
     const rt_wavefront_tuning &tc = s->cfg.tuning;
     if (tc.block_threads | tc.blocks_per_sm | tc.chunk | tc.steps | tc.stack_entries) {
-        s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk, tc.steps, tc.stack_entries,
-                                        tc.treelet ? rtd::kTreeletRecords : 0u};
+        s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk,
+                                        tc.steps,         tc.stack_entries, tc.treelet ? rtd::kTreeletRecords : 0u,
+                                        tc.shade_blocks};
         rtd::normalize_tuning(s->eng.tuning, 0u);
     }
     if (st == RT_OK) st = s->eng.reserve(s->cfg.max_slots, 64);
