@@ -777,7 +777,7 @@ def main(argv=None) -> int:
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the request-loop leg")
     ap.add_argument("--served-rate", type=float, default=10.0, help="Poisson arrival rate, jobs/s")
     ap.add_argument("--served-seconds", type=float, default=20.0, help="arrival window (s) of each rate")
-    ap.add_argument("--served-other-rates", type=lambda x: [float(v) for v in x.split(",") if v], default=[1.0, 50.0],
+    ap.add_argument("--served-other-rates", type=lambda x: [float(v) for v in x.split(",") if v], default=[1.0, 200.0],
                     help="further arrival rates of the request-loop leg (comma-separated; empty for none)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)

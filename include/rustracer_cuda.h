@@ -394,13 +394,15 @@ typedef struct rt_batch rt_batch;
  * 256, blocks_per_sm up to 2048 / block_threads, chunk (queue items a warp takes per atomic, its
  * segment of the shared queue) 32 .. 1024 in steps of 32, steps (traversal records between lane
  * refills) 1 .. 64, stack_entries 32 / 48 / 64 per lane, raised to what the jobs' trees need.
- * Default: 128 threads, 8 blocks per SM, chunk 32, 4 steps, 32 entries, no treelet, shade_blocks 6. */
+ * Default: 128 threads, 8 blocks per SM, chunk 32, 3 steps, 32 entries, no treelet, shade_blocks 6,
+ * refill_idle 0. */
 typedef struct rt_wavefront_tuning {
     uint32_t block_threads, blocks_per_sm, chunk, steps, stack_entries;
     uint32_t treelet;       /* 1: the top records of the four-wide tree are staged in shared memory */
     uint32_t shade_blocks;  /* shade kernel's register budget: 4, 5 or 6 resident blocks per SM (other
                              * values: 6) */
-    uint32_t _pad;
+    uint32_t refill_idle;   /* refill a warp's idle lanes before `steps` records once this many are idle
+                             * (0: after `steps` only) */
 } rt_wavefront_tuning;
 int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out);
 void rt_batch_destroy(rt_batch *b);

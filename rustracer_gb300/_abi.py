@@ -161,7 +161,7 @@ JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 class WavefrontTuning(C.Structure):
     _fields_ = [("block_threads", u32), ("blocks_per_sm", u32), ("chunk", u32), ("steps", u32),
-                ("stack_entries", u32), ("treelet", u32), ("shade_blocks", u32), ("_pad", u32)]
+                ("stack_entries", u32), ("treelet", u32), ("shade_blocks", u32), ("refill_idle", u32)]
 
     def as_dict(self) -> dict:
         return {f: int(getattr(self, f)) for f, _ in self._fields_ if f != "_pad"}

@@ -834,6 +834,8 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
     uint32_t id = 0;  // path slot (closest hit) or shadow record (occlusion)
     float limit = 0.0f;
     uint32_t work[4] = {0u, 0u, 0u, 0u};  // kCount: records closest / occlusion, tests closest / occlusion
+    // steps: records between refills (low 16 bits) and the idle-lane count that refills earlier (high)
+    const uint32_t max_steps = steps & 0xFFFFu, refill_idle = steps >> 16;
     for (;;) {
         const uint32_t item = warp_take(feed, !has, n_ext + n_shd, fetch, chunk);
         if (item != 0xFFFFFFFFu) {
@@ -864,7 +866,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
             if (has) warp_leaves_set_ray(wl, st);
         }
         if (!__any_sync(0xFFFFFFFFu, has)) break;
-        for (uint32_t k = 0; k < steps; ++k) {
+        for (uint32_t k = 0; k < max_steps; ++k) {
             uint32_t tests = 0u;
             const bool visiting = has;
             if (kWide ? trav_step_warp4(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr,
@@ -878,7 +880,10 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                 work[occlusion ? 1 : 0] += 1u;
                 work[occlusion ? 3 : 2] += tests;
             }
-            if (!__any_sync(0xFFFFFFFFu, has)) break;
+            const uint32_t busy = __ballot_sync(0xFFFFFFFFu, has);
+            if (busy == 0u) break;
+            // early refill once `refill_idle` lanes wait and the queue still has work
+            if (refill_idle != 0u && 32u - (uint32_t)__popc(busy) >= refill_idle && feed.more) break;
         }
     }
     if (kCount && p.work) {
@@ -955,7 +960,7 @@ __global__ void wf_count_kernel(const __grid_constant__ WaveParams p, uint32_t i
 // ------------------------------------------------------------------------------------------------
 // Host launcher: the gather pass of one frame of every job.
 // ------------------------------------------------------------------------------------------------
-WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 4u, 32u, 0u, 6u}; }
+WaveTuning default_tuning() { return WaveTuning{128u, 8u, 32u, 3u, 32u, 0u, 6u, 0u}; }
 
 bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     const WaveTuning in = t;
@@ -964,6 +969,7 @@ bool normalize_tuning(WaveTuning &t, uint32_t stack_need) {
     t.blocks_per_sm = t.blocks_per_sm < 1u ? 1u : (t.blocks_per_sm > max_blocks ? max_blocks : t.blocks_per_sm);
     t.chunk = t.chunk < 32u ? 32u : (t.chunk > 1024u ? 1024u : (t.chunk + 31u) / 32u * 32u);
     t.steps = t.steps < 1u ? 1u : (t.steps > 64u ? 64u : t.steps);
+    t.refill_idle = t.refill_idle > 31u ? 31u : t.refill_idle;
     const uint32_t need = stack_need > t.stack_entries ? stack_need : t.stack_entries;
     t.stack_entries = need <= 32u ? 32u : (need <= 48u ? 48u : 64u);
     t.treelet = t.treelet ? kTreeletRecords : 0u;
@@ -1017,9 +1023,9 @@ void trav_kernels(const WaveTuning &t, bool wide, ExtendKernel &ext, TraceKernel
 template <int kStack, int kBlock, bool kWide>
 void opt_in_smem() {
     // Blocks above 48 KB of dynamic shared memory need the opt-in; set it for every shape.
-    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 0u, 4u});
+    const int bytes = (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 0u, 4u, 0u});
     const int tree_bytes =
-        (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 1u, 4u}, true);
+        (int)trav_smem_bytes(WaveTuning{(uint32_t)kBlock, 1u, 64u, 8u, (uint32_t)kStack, 1u, 4u, 0u}, true);
     constexpr int kT = (int)kTreeletRecords;
     cudaFuncSetAttribute(wf_extend_kernel<kStack, kBlock, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(wf_trace_kernel<kStack, kBlock, kWide, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1122,7 +1128,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     };
     for (uint32_t it = 0; it < iters; ++it) {
         mark(prof ? prof->trace_ev : nullptr, n_trc, 0);
-        trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps);
+        trc<<<grid, t.block_threads, smem, st>>>(p, it, it ? it - 1u : kNoIter, t.chunk, t.steps | (t.refill_idle << 16));
         mark(prof ? prof->trace_ev : nullptr, n_trc++, 1);
         mark(prof ? prof->shade_ev : nullptr, n_shd, 0);
         shade<<<shade_grid, 128, 0, st>>>(p, it);
@@ -1135,7 +1141,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     }
     if (iters) {
         mark(prof ? prof->trace_ev : nullptr, n_trc, 0);
-        trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps);
+        trc<<<grid, t.block_threads, smem, st>>>(p, kNoIter, iters - 1u, t.chunk, t.steps | (t.refill_idle << 16));
         mark(prof ? prof->trace_ev : nullptr, n_trc++, 1);
     }
     if (prof) {

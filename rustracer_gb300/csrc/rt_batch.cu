@@ -294,7 +294,8 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
     const uint32_t per_sm[] = {2u, 4u, 6u, 8u, 12u, 16u, 24u, 32u};
     const uint32_t stacks[] = {32u, 48u, 64u};
     const uint32_t chunks[] = {32u, 64u, 128u, 256u};
-    const uint32_t steps[] = {4u, 8u, 16u, 32u};
+    const uint32_t steps[] = {3u, 4u, 8u, 16u};
+    const uint32_t refills[] = {0u, 8u, 12u};
     const uint32_t treelets[] = {0u, rtd::kTreeletRecords};
     const uint32_t shade_blocks[] = {4u, 5u, 6u};
     auto sweep = [&](uint32_t rtd::WaveTuning::*field, const uint32_t *vals, size_t nv) {
@@ -315,6 +316,7 @@ int BatchEngine::autotune(rt_renderer *const *rs, uint32_t n, uint32_t trial_fra
     sweep(&rtd::WaveTuning::stack_entries, stacks, 3);
     sweep(&rtd::WaveTuning::chunk, chunks, 4);
     sweep(&rtd::WaveTuning::steps, steps, 4);
+    sweep(&rtd::WaveTuning::refill_idle, refills, 3);
     sweep(&rtd::WaveTuning::treelet, treelets, 2);
     sweep(&rtd::WaveTuning::shade_blocks, shade_blocks, 3);
     tuning = best;
@@ -345,7 +347,8 @@ namespace {
 
 rtd::WaveTuning from_c(const rt_wavefront_tuning &t) {
     return rtd::WaveTuning{t.block_threads, t.blocks_per_sm, t.chunk,      t.steps,
-                           t.stack_entries, t.treelet ? rtd::kTreeletRecords : 0u, t.shade_blocks};
+                           t.stack_entries, t.treelet ? rtd::kTreeletRecords : 0u, t.shade_blocks,
+                           t.refill_idle};
 }
 
 void to_c(const rtd::WaveTuning &t, rt_wavefront_tuning *out) {
@@ -357,6 +360,7 @@ void to_c(const rtd::WaveTuning &t, rt_wavefront_tuning *out) {
     out->stack_entries = t.stack_entries;
     out->treelet = t.treelet ? 1u : 0u;
     out->shade_blocks = t.shade_blocks;
+    out->refill_idle = t.refill_idle;
 }
 
 }  // namespace

@@ -63,7 +63,9 @@ struct WaveTuning {
     uint32_t stack_entries;  // shared-memory stack per lane: 32, 48 or 64 (raised to the jobs' need)
     uint32_t treelet;        // four-wide records at the top of the tree staged in shared memory per
                              // block: 0 or kTreeletRecords
-    uint32_t shade_blocks;   // shade kernel compiled for 4 or 5 resident blocks of 128 per SM
+    uint32_t shade_blocks;   // shade kernel compiled for 4, 5 or 6 resident blocks of 128 per SM
+    uint32_t refill_idle;    // traversal warps refill before `steps` records once this many lanes are
+                             // idle (0: only after `steps`)
 };
 // Records of the treelet: the first records of the breadth-first four-wide layout (the root, its
 // children and most of their children), 2 KB, which fits beside 8 blocks of 128 traversal threads.

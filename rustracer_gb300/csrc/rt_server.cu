@@ -417,7 +417,7 @@ extern "C" int rt_server_create(const rt_server_config *cfg, rt_server **out) {
     if (tc.block_threads | tc.blocks_per_sm | tc.chunk | tc.steps | tc.stack_entries) {
         s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk,
                                         tc.steps,         tc.stack_entries, tc.treelet ? rtd::kTreeletRecords : 0u,
-                                        tc.shade_blocks};
+                                        tc.shade_blocks, tc.refill_idle};
         rtd::normalize_tuning(s->eng.tuning, 0u);
     }
     if (st == RT_OK) st = s->eng.reserve(s->cfg.max_slots, 64);
