@@ -33,7 +33,7 @@ extern "C" {
 #define RT_OK 0
 #define RT_ERR_INVALID_ARGUMENT 1 /* bad pointer, size or value                                 */
 #define RT_ERR_CUDA 2             /* a CUDA runtime call failed (message says which)             */
-#define RT_ERR_OUT_OF_MEMORY 3    /* device allocation failed or an admission cap was exceeded   */
+#define RT_ERR_OUT_OF_MEMORY 3    /* a device or host allocation failed, or an admission cap hit */
 #define RT_ERR_STATE 4            /* call not valid in the renderer's current state              */
 #define RT_ERR_DEVICE_CHECK 5     /* a kernel's own bounds/timeout check fired (no fault raised) */
 

@@ -679,137 +679,147 @@ extern "C" void rt_scene_destroy(rt_scene *s) { delete s; }
 extern "C" int rt_scene_add_mesh(rt_scene *s, const float *positions, const float *normals, const float *uvs,
                                  uint64_t vertex_count, const uint32_t *indices, uint64_t index_count,
                                  uint32_t material_id) {
-    if (!s || (vertex_count && !positions) || (index_count && !indices) || index_count % 3 != 0) {
-        set_error("rt_scene_add_mesh: invalid arguments (index_count must be a multiple of 3)");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    Mesh m;
-    m.positions.resize(vertex_count);
-    for (uint64_t i = 0; i < vertex_count; ++i) m.positions[i] = ld3(positions + 3 * i);
-    if (normals) {
-        m.normals.resize(vertex_count);
-        for (uint64_t i = 0; i < vertex_count; ++i) m.normals[i] = ld3(normals + 3 * i);
-    }
-    if (uvs) m.uvs.assign(uvs, uvs + 2 * vertex_count);
-    m.indices.assign(indices, indices + index_count);
-    for (uint32_t ix : m.indices)
-        if (ix >= vertex_count) {
-            set_error("rt_scene_add_mesh: index %u out of range (%llu vertices)", ix, (unsigned long long)vertex_count);
+    return rt::guarded("rt_scene_add_mesh", [&]() -> int {
+        if (!s || (vertex_count && !positions) || (index_count && !indices) || index_count % 3 != 0) {
+            set_error("rt_scene_add_mesh: invalid arguments (index_count must be a multiple of 3)");
             return RT_ERR_INVALID_ARGUMENT;
         }
-    m.material_id = material_id;
-    s->meshes.push_back(std::move(m));
-    s->finalized = false;
-    return RT_OK;
+        Mesh m;
+        m.positions.resize(vertex_count);
+        for (uint64_t i = 0; i < vertex_count; ++i) m.positions[i] = ld3(positions + 3 * i);
+        if (normals) {
+            m.normals.resize(vertex_count);
+            for (uint64_t i = 0; i < vertex_count; ++i) m.normals[i] = ld3(normals + 3 * i);
+        }
+        if (uvs) m.uvs.assign(uvs, uvs + 2 * vertex_count);
+        m.indices.assign(indices, indices + index_count);
+        for (uint32_t ix : m.indices)
+            if (ix >= vertex_count) {
+                set_error("rt_scene_add_mesh: index %u out of range (%llu vertices)", ix, (unsigned long long)vertex_count);
+                return RT_ERR_INVALID_ARGUMENT;
+            }
+        m.material_id = material_id;
+        s->meshes.push_back(std::move(m));
+        s->finalized = false;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_scene_add_material(rt_scene *s, const rt_material *m) {
-    if (!s || !m) {
-        set_error("rt_scene_add_material: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    s->materials.push_back(*m);
-    s->finalized = false;
-    return RT_OK;
+    return rt::guarded("rt_scene_add_material", [&]() -> int {
+        if (!s || !m) {
+            set_error("rt_scene_add_material: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        s->materials.push_back(*m);
+        s->finalized = false;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_scene_add_light(rt_scene *s, const rt_light *l) {
-    if (!s || !l) {
-        set_error("rt_scene_add_light: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    s->lights.push_back(*l);
-    s->finalized = false;
-    return RT_OK;
+    return rt::guarded("rt_scene_add_light", [&]() -> int {
+        if (!s || !l) {
+            set_error("rt_scene_add_light: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        s->lights.push_back(*l);
+        s->finalized = false;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_scene_set_textures(rt_scene *s, int role, const uint8_t *rgba8, uint32_t width, uint32_t height,
                                      uint32_t layers) {
-    if (!s || role < 0 || role > 3 || (layers && (!rgba8 || !width || !height))) {
-        set_error("rt_scene_set_textures: invalid arguments");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    Texture &t = s->tex[role];
-    t.width = layers ? width : 0;
-    t.height = layers ? height : 0;
-    t.layers = layers;
-    t.rgba8.assign(rgba8, rgba8 + (size_t)width * height * layers * 4 * (layers ? 1 : 0));
-    return RT_OK;
+    return rt::guarded("rt_scene_set_textures", [&]() -> int {
+        if (!s || role < 0 || role > 3 || (layers && (!rgba8 || !width || !height))) {
+            set_error("rt_scene_set_textures: invalid arguments");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        Texture &t = s->tex[role];
+        t.width = layers ? width : 0;
+        t.height = layers ? height : 0;
+        t.layers = layers;
+        t.rgba8.assign(rgba8, rgba8 + (size_t)width * height * layers * 4 * (layers ? 1 : 0));
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_scene_finalize(rt_scene *s) {
-    if (!s) {
-        set_error("rt_scene_finalize: null scene");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (s->finalized) return RT_OK;
-    size_t ntri = 0;
-    for (const auto &m : s->meshes) ntri += m.indices.size() / 3;
-    if (ntri > 0xFFFFFFFFull) {
-        set_error("rt_scene_finalize: too many triangles");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    s->triangles.clear();
-    s->triangles.reserve(ntri);
-    std::vector<Vec3> centroids, bmin, bmax;
-    centroids.reserve(ntri);
-    bmin.reserve(ntri);
-    bmax.reserve(ntri);
-    Vec3 mn{F32_MAX, F32_MAX, F32_MAX}, mx{-F32_MAX, -F32_MAX, -F32_MAX};
-    for (const auto &m : s->meshes) {
-        for (const auto &p : m.positions) {
-            mn = {std::fmin(mn.x, p.x), std::fmin(mn.y, p.y), std::fmin(mn.z, p.z)};
-            mx = {std::fmax(mx.x, p.x), std::fmax(mx.y, p.y), std::fmax(mx.z, p.z)};
+    return rt::guarded("rt_scene_finalize", [&]() -> int {
+        if (!s) {
+            set_error("rt_scene_finalize: null scene");
+            return RT_ERR_INVALID_ARGUMENT;
         }
-        size_t nv = m.positions.size();
-        for (size_t t = 0; t + 2 < m.indices.size(); t += 3) {
-            uint32_t ix[3] = {m.indices[t], m.indices[t + 1], m.indices[t + 2]};
-            rt_triangle tri;
-            std::memset(&tri, 0, sizeof(tri));
-            float *vv[3] = {tri.v0, tri.v1, tri.v2};
-            float *nn[3] = {tri.n0, tri.n1, tri.n2};
-            float *uu[3] = {tri.uv0, tri.uv1, tri.uv2};
-            Vec3 p[3];
-            for (int k = 0; k < 3; ++k) {
-                p[k] = ix[k] < nv ? m.positions[ix[k]] : Vec3{0, 0, 0};
-                st3(vv[k], p[k]);
-                Vec3 n = ix[k] < m.normals.size() ? m.normals[ix[k]] : Vec3{0, 1, 0};
-                st3(nn[k], n);
-                if ((size_t)ix[k] * 2 + 1 < m.uvs.size()) {
-                    uu[k][0] = m.uvs[2 * ix[k]];
-                    uu[k][1] = m.uvs[2 * ix[k] + 1];
+        if (s->finalized) return RT_OK;
+        size_t ntri = 0;
+        for (const auto &m : s->meshes) ntri += m.indices.size() / 3;
+        if (ntri > 0xFFFFFFFFull) {
+            set_error("rt_scene_finalize: too many triangles");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        s->triangles.clear();
+        s->triangles.reserve(ntri);
+        std::vector<Vec3> centroids, bmin, bmax;
+        centroids.reserve(ntri);
+        bmin.reserve(ntri);
+        bmax.reserve(ntri);
+        Vec3 mn{F32_MAX, F32_MAX, F32_MAX}, mx{-F32_MAX, -F32_MAX, -F32_MAX};
+        for (const auto &m : s->meshes) {
+            for (const auto &p : m.positions) {
+                mn = {std::fmin(mn.x, p.x), std::fmin(mn.y, p.y), std::fmin(mn.z, p.z)};
+                mx = {std::fmax(mx.x, p.x), std::fmax(mx.y, p.y), std::fmax(mx.z, p.z)};
+            }
+            size_t nv = m.positions.size();
+            for (size_t t = 0; t + 2 < m.indices.size(); t += 3) {
+                uint32_t ix[3] = {m.indices[t], m.indices[t + 1], m.indices[t + 2]};
+                rt_triangle tri;
+                std::memset(&tri, 0, sizeof(tri));
+                float *vv[3] = {tri.v0, tri.v1, tri.v2};
+                float *nn[3] = {tri.n0, tri.n1, tri.n2};
+                float *uu[3] = {tri.uv0, tri.uv1, tri.uv2};
+                Vec3 p[3];
+                for (int k = 0; k < 3; ++k) {
+                    p[k] = ix[k] < nv ? m.positions[ix[k]] : Vec3{0, 0, 0};
+                    st3(vv[k], p[k]);
+                    Vec3 n = ix[k] < m.normals.size() ? m.normals[ix[k]] : Vec3{0, 1, 0};
+                    st3(nn[k], n);
+                    if ((size_t)ix[k] * 2 + 1 < m.uvs.size()) {
+                        uu[k][0] = m.uvs[2 * ix[k]];
+                        uu[k][1] = m.uvs[2 * ix[k] + 1];
+                    }
                 }
+                tri.material_id = m.tri_materials.empty() ? m.material_id : m.tri_materials[t / 3];
+                s->triangles.push_back(tri);
+                // Mesh::triangle_centroid / triangle_aabb (scene.rs:62-70)
+                centroids.push_back((p[0] + p[1] + p[2]) / 3.0f);
+                Vec3 lo{F32_MAX, F32_MAX, F32_MAX}, hi{-F32_MAX, -F32_MAX, -F32_MAX};
+                for (int k = 0; k < 3; ++k) {
+                    lo = {std::fmin(lo.x, p[k].x), std::fmin(lo.y, p[k].y), std::fmin(lo.z, p[k].z)};
+                    hi = {std::fmax(hi.x, p[k].x), std::fmax(hi.y, p[k].y), std::fmax(hi.z, p[k].z)};
+                }
+                bmin.push_back(lo);
+                bmax.push_back(hi);
             }
-            tri.material_id = m.tri_materials.empty() ? m.material_id : m.tri_materials[t / 3];
-            s->triangles.push_back(tri);
-            // Mesh::triangle_centroid / triangle_aabb (scene.rs:62-70)
-            centroids.push_back((p[0] + p[1] + p[2]) / 3.0f);
-            Vec3 lo{F32_MAX, F32_MAX, F32_MAX}, hi{-F32_MAX, -F32_MAX, -F32_MAX};
-            for (int k = 0; k < 3; ++k) {
-                lo = {std::fmin(lo.x, p[k].x), std::fmin(lo.y, p[k].y), std::fmin(lo.z, p[k].z)};
-                hi = {std::fmax(hi.x, p[k].x), std::fmax(hi.y, p[k].y), std::fmax(hi.z, p[k].z)};
+        }
+        s->bvh_builder_used = RT_BVH_HOST_SAH;
+        if (s->bvh_builder == RT_BVH_GPU_LBVH && ntri >= 2 && rt_device_count() > 0) {
+            static_assert(sizeof(Vec3) == 12, "Vec3 arrays are read as packed floats");
+            uint32_t depth = 0;
+            rt::BVH b;
+            // The traversal stack holds at most 63 pending nodes: deeper trees take the host build.
+            if (rtd::build_lbvh(&centroids[0].x, &bmin[0].x, &bmax[0].x, (uint32_t)ntri, b, &depth) == 0 && depth <= 62) {
+                s->bvh = std::move(b);
+                s->bvh_builder_used = RT_BVH_GPU_LBVH;
             }
-            bmin.push_back(lo);
-            bmax.push_back(hi);
         }
-    }
-    s->bvh_builder_used = RT_BVH_HOST_SAH;
-    if (s->bvh_builder == RT_BVH_GPU_LBVH && ntri >= 2 && rt_device_count() > 0) {
-        static_assert(sizeof(Vec3) == 12, "Vec3 arrays are read as packed floats");
-        uint32_t depth = 0;
-        rt::BVH b;
-        // The traversal stack holds at most 63 pending nodes: deeper trees take the host build.
-        if (rtd::build_lbvh(&centroids[0].x, &bmin[0].x, &bmax[0].x, (uint32_t)ntri, b, &depth) == 0 && depth <= 62) {
-            s->bvh = std::move(b);
-            s->bvh_builder_used = RT_BVH_GPU_LBVH;
-        }
-    }
-    if (s->bvh_builder_used == RT_BVH_HOST_SAH) s->bvh = build_bvh(centroids, bmin, bmax);
-    s->has_bounds = !(mn.x > mx.x);
-    st3(s->bounds_min, s->has_bounds ? mn : Vec3{0, 0, 0});
-    st3(s->bounds_max, s->has_bounds ? mx : Vec3{0, 0, 0});
-    s->finalized = true;
-    return RT_OK;
+        if (s->bvh_builder_used == RT_BVH_HOST_SAH) s->bvh = build_bvh(centroids, bmin, bmax);
+        s->has_bounds = !(mn.x > mx.x);
+        st3(s->bounds_min, s->has_bounds ? mn : Vec3{0, 0, 0});
+        st3(s->bounds_max, s->has_bounds ? mx : Vec3{0, 0, 0});
+        s->finalized = true;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_scene_describe(rt_scene *s, rt_scene_desc *d) {
@@ -858,38 +868,38 @@ extern "C" uint64_t rt_scene_triangle_count(const rt_scene *s) {
 // ================================================================================================
 extern "C" int rt_bvh_build(const float *centroids, const float *bbox_min, const float *bbox_max, uint64_t n,
                             rt_bvh **out) {
-    if (!out || (n && (!centroids || !bbox_min || !bbox_max)) || n > 0xFFFFFFFFull) {
-        set_error("rt_bvh_build: invalid arguments");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::vector<Vec3> c(n), lo(n), hi(n);
-    for (uint64_t i = 0; i < n; ++i) {
-        c[i] = ld3(centroids + 3 * i);
-        lo[i] = ld3(bbox_min + 3 * i);
-        hi[i] = ld3(bbox_max + 3 * i);
-    }
-    rt_bvh *b = new (std::nothrow) rt_bvh();
-    if (!b) {
-        set_error("rt_bvh_build: out of host memory");
-        return RT_ERR_OUT_OF_MEMORY;
-    }
-    b->b = build_bvh(c, lo, hi);
-    *out = b;
-    return RT_OK;
+    return rt::guarded("rt_bvh_build", [&]() -> int {
+        if (!out || (n && (!centroids || !bbox_min || !bbox_max)) || n > 0xFFFFFFFFull) {
+            set_error("rt_bvh_build: invalid arguments");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::vector<Vec3> c(n), lo(n), hi(n);
+        for (uint64_t i = 0; i < n; ++i) {
+            c[i] = ld3(centroids + 3 * i);
+            lo[i] = ld3(bbox_min + 3 * i);
+            hi[i] = ld3(bbox_max + 3 * i);
+        }
+        std::unique_ptr<rt_bvh> b(new rt_bvh());
+        b->b = build_bvh(c, lo, hi);
+        *out = b.release();
+        return RT_OK;
+    });
 }
 extern "C" int rt_bvh_wide_layout(const rt_bvh_node *nodes, uint64_t n_nodes, float *out, uint64_t capacity,
                                   uint64_t *records, uint32_t *stack_need) {
-    rt::clear_error();
-    if ((!nodes && n_nodes) || !records || !stack_need) {
-        rt::set_error("rt_bvh_wide_layout: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    rt::WideLayout w;
-    rt::build_wide_layout(nodes, n_nodes, w);
-    *records = w.nodes.size() / 32;
-    *stack_need = w.stack_need;
-    if (out) std::memcpy(out, w.nodes.data(), sizeof(float) * std::min<uint64_t>(capacity, w.nodes.size()));
-    return RT_OK;
+    return rt::guarded("rt_bvh_wide_layout", [&]() -> int {
+        rt::clear_error();
+        if ((!nodes && n_nodes) || !records || !stack_need) {
+            rt::set_error("rt_bvh_wide_layout: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        rt::WideLayout w;
+        rt::build_wide_layout(nodes, n_nodes, w);
+        *records = w.nodes.size() / 32;
+        *stack_need = w.stack_need;
+        if (out) std::memcpy(out, w.nodes.data(), sizeof(float) * std::min<uint64_t>(capacity, w.nodes.size()));
+        return RT_OK;
+    });
 }
 
 extern "C" const rt_bvh_node *rt_bvh_nodes(const rt_bvh *b, uint64_t *count) {
@@ -995,10 +1005,26 @@ static void add_rotated_box(rt_scene *s, float sx, float sy, float sz, double de
     add_box(s, c, mat);
 }
 
-extern "C" int rt_scene_create_cornell555(rt_scene **out) {
+// Creates a scene and fills it; a fill that fails (or throws) leaves *out null and nothing allocated.
+template <class F>
+static int generate_scene(const char *fn, rt_scene **out, F &&fill) {
     int st = rt_scene_create(out);
     if (st != RT_OK) return st;
-    rt_scene *s = *out;
+    st = rt::guarded(fn, [&]() -> int { return fill(*out); });
+    if (st != RT_OK) {
+        rt_scene_destroy(*out);
+        *out = nullptr;
+    }
+    return st;
+}
+
+static int fill_cornell555(rt_scene *s);
+
+extern "C" int rt_scene_create_cornell555(rt_scene **out) {
+    return generate_scene("rt_scene_create_cornell555", out, fill_cornell555);
+}
+
+static int fill_cornell555(rt_scene *s) {
     s->materials.push_back(mat_lambertian(0.73f, 0.73f, 0.73f));      // 0 white
     s->materials.push_back(mat_lambertian(0.65f, 0.05f, 0.05f));      // 1 red
     s->materials.push_back(mat_lambertian(0.12f, 0.45f, 0.15f));      // 2 green
@@ -1057,15 +1083,19 @@ static void value_noise(std::vector<float> &out, uint32_t size, uint32_t cells, 
 // create_role_array's quantisation (lib.rs:1315-1326): (clamp(c, 0, 1) * 255) as u8, truncating.
 static inline uint8_t quant(float c) { return (uint8_t)(std::fmin(std::fmax(c, 0.0f), 1.0f) * 255.0f); }
 
+static int fill_icosphere_room(rt_scene *s, uint32_t level, uint64_t seed, float sigma, uint32_t tex_size);
+
 extern "C" int rt_scene_create_icosphere_room(uint32_t level, uint64_t seed, float sigma, uint32_t tex_size,
                                               rt_scene **out) {
     if (level > 10 || tex_size > 8192) {
         set_error("rt_scene_create_icosphere_room: level must be <= 10 and tex_size <= 8192");
         return RT_ERR_INVALID_ARGUMENT;
     }
-    int st = rt_scene_create(out);
-    if (st != RT_OK) return st;
-    rt_scene *s = *out;
+    return generate_scene("rt_scene_create_icosphere_room", out,
+                          [&](rt_scene *s) { return fill_icosphere_room(s, level, seed, sigma, tex_size); });
+}
+
+static int fill_icosphere_room(rt_scene *s, uint32_t level, uint64_t seed, float sigma, uint32_t tex_size) {
     HostRng rng(seed * 0x2545F4914F6CDD1Dull + 0x1234567ull);
 
     // --- icosahedron, subdivided `level` times, projected to the unit sphere -------------------
@@ -1301,21 +1331,18 @@ extern "C" uint32_t rt_scene_bvh_builder_used(const rt_scene *s) { return s ? s-
 
 extern "C" int rt_bvh_build_gpu(const float *centroids, const float *bbox_min, const float *bbox_max, uint64_t n,
                                 rt_bvh **out, uint32_t *max_depth) {
-    rt::clear_error();
-    if (!out || n < 2 || n > 0x7FFFFFFFull || !centroids || !bbox_min || !bbox_max) {
-        set_error("rt_bvh_build_gpu: need 2 .. 2^31 - 1 primitives and their centroids and boxes");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    rt_bvh *b = new (std::nothrow) rt_bvh();
-    if (!b) {
-        set_error("rt_bvh_build_gpu: out of host memory");
-        return RT_ERR_OUT_OF_MEMORY;
-    }
-    if (rtd::build_lbvh(centroids, bbox_min, bbox_max, (uint32_t)n, b->b, max_depth) != 0) {
-        delete b;
-        set_error("rt_bvh_build_gpu: a CUDA call failed");
-        return RT_ERR_CUDA;
-    }
-    *out = b;
-    return RT_OK;
+    return rt::guarded("rt_bvh_build_gpu", [&]() -> int {
+        rt::clear_error();
+        if (!out || n < 2 || n > 0x7FFFFFFFull || !centroids || !bbox_min || !bbox_max) {
+            set_error("rt_bvh_build_gpu: need 2 .. 2^31 - 1 primitives and their centroids and boxes");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::unique_ptr<rt_bvh> b(new rt_bvh());
+        if (rtd::build_lbvh(centroids, bbox_min, bbox_max, (uint32_t)n, b->b, max_depth) != 0) {
+            set_error("rt_bvh_build_gpu: a CUDA call failed");
+            return RT_ERR_CUDA;
+        }
+        *out = b.release();
+        return RT_OK;
+    });
 }

@@ -3,6 +3,8 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -18,6 +20,21 @@ void set_error(const char *fmt, ...)
 #endif
     ;
 void clear_error();
+
+// Runs the body of a C entry point so that no C++ exception crosses the C ABI: an allocation
+// failure becomes RT_ERR_OUT_OF_MEMORY, any other exception RT_ERR_STATE, each with a message.
+template <class F>
+int guarded(const char *fn, F &&body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        set_error("%s: out of host memory", fn);
+        return RT_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        set_error("%s: %s", fn, e.what());
+        return RT_ERR_STATE;
+    }
+}
 
 struct Vec3 {
     float x, y, z;

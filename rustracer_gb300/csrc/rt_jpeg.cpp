@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "rt_internal.h"
@@ -502,8 +503,15 @@ extern "C" int rt_jpeg_decode(const uint8_t *data, uint64_t n, uint8_t *out_rgba
     }
     std::vector<uint8_t> rgba;
     uint32_t ww = 0, hh = 0;
-    Decoder dec(data, (size_t)n);
-    if (!dec.decode(rgba, ww, hh)) {
+    bool ok = false;
+    try {  // a huge declared frame can exhaust host memory; no exception crosses the C ABI
+        Decoder dec(data, (size_t)n);
+        ok = dec.decode(rgba, ww, hh);
+    } catch (const std::bad_alloc &) {
+        rt::set_error("rt_jpeg_decode: out of host memory for a %ux%u image", ww, hh);
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    if (!ok) {
         rt::set_error("rt_jpeg_decode: not a JPEG stream this decoder handles (baseline / extended / progressive "
                       "Huffman, 8-bit, 1 or 3 components)");
         return RT_ERR_INVALID_ARGUMENT;

@@ -153,6 +153,21 @@ def test_invalid_arguments(lib):
     assert lib.rt_stage_denoise(None, None, None, 4, 4, 1.0, 2, None) == A.RT_ERR_INVALID_ARGUMENT
 
 
+def test_no_exception_crosses_the_c_abi(lib):
+    """A vertex count no vector can hold makes the mesh copy throw before anything is read; the entry
+    point returns an error code with a message instead of unwinding into the caller."""
+    s = rt.Scene()
+    pos = np.zeros((3, 3), np.float32)
+    idx = np.array([0, 1, 2], np.uint32)
+    st = lib.rt_scene_add_mesh(s.handle, A.ptr(pos), None, None, 1 << 63, A.ptr(idx), 3, 0)
+    assert st in (A.RT_ERR_STATE, A.RT_ERR_OUT_OF_MEMORY)
+    assert b"rt_scene_add_mesh" in lib.rt_last_error()
+    assert s.triangle_count() == 0  # the failed call added nothing
+    s.add_material(rt.lambertian((0.5, 0.5, 0.5)))
+    s.add_mesh(pos + np.eye(3, dtype=np.float32), idx, 0)  # the scene is still usable
+    assert s.triangle_count() == 1
+
+
 def test_mesh_defaults(lib):
     """flatten_triangles (scene.rs:213-273): missing normals -> +Y, missing uvs -> (0, 0)."""
     s = rt.Scene()
