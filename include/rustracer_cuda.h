@@ -489,6 +489,8 @@ int rt_server_create(const rt_server_config *cfg, rt_server **out);
 /* Stops the worker after the frames in flight; queued jobs are dropped. */
 void rt_server_destroy(rt_server *s);
 int rt_server_add_scene(rt_server *s, uint32_t scene_id, const rt_scene_desc *scene);
+/* Queues a job.  RT_ERR_STATE once the worker thread has stopped on a host allocation failure (it
+ * then fails every job not yet done, so rt_server_wait_idle returns). */
 int rt_server_submit(rt_server *s, const rt_request *req, uint64_t *job_id);
 int rt_server_job_status(rt_server *s, uint64_t job_id, rt_job_status *out);
 /* The final accumulation (W*H*4 floats) of a done job submitted with keep_result. */

@@ -371,125 +371,145 @@ struct rt_batch {
 };
 
 extern "C" int rt_batch_create(rt_renderer *const *renderers, uint32_t n, uint32_t use_graphs, rt_batch **out) {
-    rt::clear_error();
-    if (!out || !renderers || n == 0 || n > (1u << 15)) {
-        set_error("rt_batch_create: need 1 .. 32768 renderers");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    rt_batch *b = new (std::nothrow) rt_batch();
-    if (!b) {
-        set_error("rt_batch_create: out of host memory");
-        return RT_ERR_OUT_OF_MEMORY;
-    }
-    auto fail = [&](int st) {
-        delete b;
-        return st;
-    };
-    uint64_t slots = 0;
-    for (uint32_t j = 0; j < n; ++j) {
-        if (!renderers[j]) {
-            set_error("rt_batch_create: renderer %u is null", j);
-            return fail(RT_ERR_INVALID_ARGUMENT);
+    return rt::guarded("rt_batch_create", [&]() -> int {
+        rt::clear_error();
+        if (!out || !renderers || n == 0 || n > (1u << 15)) {
+            set_error("rt_batch_create: need 1 .. 32768 renderers");
+            return RT_ERR_INVALID_ARGUMENT;
         }
-        for (uint32_t k = 0; k < j; ++k)
-            if (renderers[k] == renderers[j]) {
-                set_error("rt_batch_create: renderer %u appears twice", j);
+        *out = nullptr;
+        rt_batch *b = new (std::nothrow) rt_batch();
+        if (!b) {
+            set_error("rt_batch_create: out of host memory");
+            return RT_ERR_OUT_OF_MEMORY;
+        }
+        auto fail = [&](int st) {
+            delete b;
+            return st;
+        };
+        uint64_t slots = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            if (!renderers[j]) {
+                set_error("rt_batch_create: renderer %u is null", j);
                 return fail(RT_ERR_INVALID_ARGUMENT);
             }
-        b->rs.push_back(renderers[j]);
-        slots += (uint64_t)renderers[j]->cfg.width * renderers[j]->cfg.height;
-        if (slots > 0xFFFFFFFFull) {
-            set_error("rt_batch_create: the jobs' pixels exceed 2^32");
-            return fail(RT_ERR_INVALID_ARGUMENT);
+            for (uint32_t k = 0; k < j; ++k)
+                if (renderers[k] == renderers[j]) {
+                    set_error("rt_batch_create: renderer %u appears twice", j);
+                    return fail(RT_ERR_INVALID_ARGUMENT);
+                }
+            b->rs.push_back(renderers[j]);
+            slots += (uint64_t)renderers[j]->cfg.width * renderers[j]->cfg.height;
+            if (slots > 0xFFFFFFFFull) {
+                set_error("rt_batch_create: the jobs' pixels exceed 2^32");
+                return fail(RT_ERR_INVALID_ARGUMENT);
+            }
         }
-    }
-    if (int st = b->eng.init(n, use_graphs ? rt::GraphMode::Always : rt::GraphMode::Off)) return fail(st);
-    *out = b;
-    return RT_OK;
+        if (int st = b->eng.init(n, use_graphs ? rt::GraphMode::Always : rt::GraphMode::Off)) return fail(st);
+        *out = b;
+        return RT_OK;
+    });
 }
 
 extern "C" void rt_batch_destroy(rt_batch *b) { delete b; }
 
 extern "C" int rt_batch_render_frame(rt_batch *b) {
-    if (!b) {
-        set_error("rt_batch_render_frame: null batch");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    rt::clear_error();
-    return b->eng.frame(b->rs.data(), (uint32_t)b->rs.size());
+    return rt::guarded("rt_batch_render_frame", [&]() -> int {
+        if (!b) {
+            set_error("rt_batch_render_frame: null batch");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        rt::clear_error();
+        return b->eng.frame(b->rs.data(), (uint32_t)b->rs.size());
+    });
 }
 
 extern "C" int rt_batch_render_frames(rt_batch *b, uint32_t n) {
-    for (uint32_t i = 0; i < n; ++i)
-        if (int st = rt_batch_render_frame(b)) return st;
-    return RT_OK;
+    return rt::guarded("rt_batch_render_frames", [&]() -> int {
+        for (uint32_t i = 0; i < n; ++i)
+            if (int st = rt_batch_render_frame(b)) return st;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_batch_synchronize(rt_batch *b) {
-    if (!b) {
-        set_error("rt_batch_synchronize: null batch");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    RT_CK(cudaStreamSynchronize(b->eng.stream));
-    return RT_OK;
+    return rt::guarded("rt_batch_synchronize", [&]() -> int {
+        if (!b) {
+            set_error("rt_batch_synchronize: null batch");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        RT_CK(cudaStreamSynchronize(b->eng.stream));
+        return RT_OK;
+    });
 }
 
 extern "C" void *rt_batch_stream(rt_batch *b) { return b ? (void *)b->eng.stream : nullptr; }
 
 extern "C" int rt_batch_get_stats(rt_batch *b, rt_frame_stats *out) {
-    if (!b || !out) {
-        set_error("rt_batch_get_stats: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    return b->eng.stats(out);
+    return rt::guarded("rt_batch_get_stats", [&]() -> int {
+        if (!b || !out) {
+            set_error("rt_batch_get_stats: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        return b->eng.stats(out);
+    });
 }
 
 extern "C" int rt_batch_set_tuning(rt_batch *b, const rt_wavefront_tuning *t) {
-    if (!b || !t) {
-        set_error("rt_batch_set_tuning: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    b->eng.tuning = from_c(*t);
-    rtd::normalize_tuning(b->eng.tuning, 0u);
-    return RT_OK;
+    return rt::guarded("rt_batch_set_tuning", [&]() -> int {
+        if (!b || !t) {
+            set_error("rt_batch_set_tuning: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        b->eng.tuning = from_c(*t);
+        rtd::normalize_tuning(b->eng.tuning, 0u);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_batch_get_tuning(rt_batch *b, rt_wavefront_tuning *t) {
-    if (!b || !t) {
-        set_error("rt_batch_get_tuning: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    to_c(b->eng.tuning, t);
-    return RT_OK;
+    return rt::guarded("rt_batch_get_tuning", [&]() -> int {
+        if (!b || !t) {
+            set_error("rt_batch_get_tuning: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        to_c(b->eng.tuning, t);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_batch_autotune(rt_batch *b, uint32_t trial_frames, rt_wavefront_tuning *best, float *best_ms) {
-    if (!b) {
-        set_error("rt_batch_autotune: null batch");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    rt::clear_error();
-    const int st = b->eng.autotune(b->rs.data(), (uint32_t)b->rs.size(), trial_frames, best_ms);
-    if (best) to_c(b->eng.tuning, best);
-    return st;
+    return rt::guarded("rt_batch_autotune", [&]() -> int {
+        if (!b) {
+            set_error("rt_batch_autotune: null batch");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        rt::clear_error();
+        const int st = b->eng.autotune(b->rs.data(), (uint32_t)b->rs.size(), trial_frames, best_ms);
+        if (best) to_c(b->eng.tuning, best);
+        return st;
+    });
 }
 
 extern "C" int rt_set_tuning(rt_renderer *r, const rt_wavefront_tuning *t) {
-    if (!r || !t) {
-        set_error("rt_set_tuning: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    r->tuning = from_c(*t);
-    rtd::normalize_tuning(r->tuning, 0u);
-    return RT_OK;
+    return rt::guarded("rt_set_tuning", [&]() -> int {
+        if (!r || !t) {
+            set_error("rt_set_tuning: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        r->tuning = from_c(*t);
+        rtd::normalize_tuning(r->tuning, 0u);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_get_tuning(const rt_renderer *r, rt_wavefront_tuning *t) {
-    if (!r || !t) {
-        set_error("rt_get_tuning: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    to_c(r->tuning, t);
-    return RT_OK;
+    return rt::guarded("rt_get_tuning", [&]() -> int {
+        if (!r || !t) {
+            set_error("rt_get_tuning: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        to_c(r->tuning, t);
+        return RT_OK;
+    });
 }

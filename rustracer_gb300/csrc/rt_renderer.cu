@@ -371,14 +371,16 @@ uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, ui
 }  // namespace rt
 
 extern "C" int rt_resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
-    rt::clear_error();
-    if (!sd || !out) {
-        set_error("rt_resident_scene_create: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    if (int st = check_scene_desc(sd, "rt_resident_scene_create")) return st;
-    return rt::resident_scene_create(sd, out);
+    return rt::guarded("rt_resident_scene_create", [&]() -> int {
+        rt::clear_error();
+        if (!sd || !out) {
+            set_error("rt_resident_scene_create: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        *out = nullptr;
+        if (int st = check_scene_desc(sd, "rt_resident_scene_create")) return st;
+        return rt::resident_scene_create(sd, out);
+    });
 }
 
 extern "C" void rt_resident_scene_release(rt_resident_scene *s) { rt::resident_scene_release(s); }
@@ -388,30 +390,34 @@ extern "C" uint64_t rt_resident_scene_bytes(const rt_resident_scene *s) { return
 extern "C" uint32_t rt_resident_scene_refs(const rt_resident_scene *s) { return s ? s->refs.load() : 0u; }
 
 extern "C" int rt_renderer_create_resident(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer **out) {
-    rt::clear_error();
-    if (!res || !cfg || !out) {
-        set_error("rt_renderer_create_resident: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    if (int st = check_config(cfg, "rt_renderer_create_resident")) return st;
-    return create_on(res, cfg, out);
+    return rt::guarded("rt_renderer_create_resident", [&]() -> int {
+        rt::clear_error();
+        if (!res || !cfg || !out) {
+            set_error("rt_renderer_create_resident: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        *out = nullptr;
+        if (int st = check_config(cfg, "rt_renderer_create_resident")) return st;
+        return create_on(res, cfg, out);
+    });
 }
 
 extern "C" int rt_renderer_create(const rt_scene_desc *sd, const rt_render_config *cfg, rt_renderer **out) {
-    rt::clear_error();
-    if (!sd || !cfg || !out) {
-        set_error("rt_renderer_create: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    if (int st = check_config(cfg, "rt_renderer_create")) return st;
-    if (int st = check_scene_desc(sd, "rt_renderer_create")) return st;
-    rt_resident_scene *res = nullptr;
-    if (int st = rt::resident_scene_create(sd, &res)) return st;
-    const int st = create_on(res, cfg, out);
-    rt::resident_scene_release(res);  // the renderer holds its own reference
-    return st;
+    return rt::guarded("rt_renderer_create", [&]() -> int {
+        rt::clear_error();
+        if (!sd || !cfg || !out) {
+            set_error("rt_renderer_create: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        *out = nullptr;
+        if (int st = check_config(cfg, "rt_renderer_create")) return st;
+        if (int st = check_scene_desc(sd, "rt_renderer_create")) return st;
+        rt_resident_scene *res = nullptr;
+        if (int st = rt::resident_scene_create(sd, &res)) return st;
+        const int st = create_on(res, cfg, out);
+        rt::resident_scene_release(res);  // the renderer holds its own reference
+        return st;
+    });
 }
 
 extern "C" uint64_t rt_renderer_device_bytes(const rt_renderer *r) { return r ? r->device_bytes() : 0; }
@@ -421,22 +427,24 @@ extern "C" uint32_t rt_scan_timeouts(void) { return rtd::scan_timeouts(); }
 
 extern "C" int rt_renderer_footprint(const rt_render_config *cfg, const rt_resident_scene *res, uint64_t *create_bytes,
                                      uint64_t *solo_path_bytes) {
-    rt::clear_error();
-    if (!cfg || !res || !create_bytes) {
-        set_error("rt_renderer_footprint: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (int st = check_config(cfg, "rt_renderer_footprint")) return st;
-    rt_grid_params gp;
-    float radius = cfg->photon_radius;
-    rt_derive_grid(res->bmin, res->bmax, (int)res->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
-                   (uint32_t)photon_slots_of(*cfg), &gp, &radius);
-    *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells, res->lights.size());
-    if (solo_path_bytes) {
-        const uint32_t spp = cfg->spp > 1u ? cfg->spp : 1u;
-        *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg));
-    }
-    return RT_OK;
+    return rt::guarded("rt_renderer_footprint", [&]() -> int {
+        rt::clear_error();
+        if (!cfg || !res || !create_bytes) {
+            set_error("rt_renderer_footprint: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if (int st = check_config(cfg, "rt_renderer_footprint")) return st;
+        rt_grid_params gp;
+        float radius = cfg->photon_radius;
+        rt_derive_grid(res->bmin, res->bmax, (int)res->has_bounds, cfg->grid_max_dim, cfg->photon_radius_mode,
+                       (uint32_t)photon_slots_of(*cfg), &gp, &radius);
+        *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells, res->lights.size());
+        if (solo_path_bytes) {
+            const uint32_t spp = cfg->spp > 1u ? cfg->spp : 1u;
+            *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg));
+        }
+        return RT_OK;
+    });
 }
 
 extern "C" void rt_renderer_destroy(rt_renderer *r) { delete r; }
@@ -530,50 +538,52 @@ int enqueue_post(rt_renderer *r, float alpha, const float *alpha_dev, cudaStream
 }  // namespace rt
 
 extern "C" int rt_render_frame(rt_renderer *r) {
-    if (int st = check_renderer(r, "rt_render_frame")) return st;
-    rt::clear_error();
-    cudaStream_t s = r->stream;
-    const rt_render_config &c = r->cfg;
-    const float alpha = rt::prepare_frame(r);
-    const uint32_t iters = rt::frame_iterations(r);
-    const size_t npix = (size_t)c.width * c.height;
-    if (npix > r->path.slots || sizeof(uint32_t) * 4 * ((size_t)iters + 1) > r->path.counts_bytes) {
-        RT_CK(cudaStreamSynchronize(s));
-        RT_CK(r->path.ensure(npix, iters));
-    }
-    cudaEvent_t fe[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (auto &e : fe) RT_CK(r->ring.next(&e));
-    RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
-    const rtd::DevJob job = rt::make_job(r, 0u);
-    RT_CK(r->jobs.upload(&job, 1, s));
-    const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
-    const rtd::JobShape shape{c.width,
-                              c.height,
-                              (uint32_t)npix,
-                              0u,
-                              r->scene.stack_cap,
-                              c.enable_photon_map ? 1u : 0u,
-                              c.debug_view != 0u ? 1u : 0u,
-                              r->scene.wnodes ? 1u : 0u,
-                              r->scene.wide_stack};
-    if (r->prof_flags) {
-        if (int st = rt::profiled_gather(r, wp, shape, iters)) return st;
-    } else {
-        RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
-    }
-    RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
-    float4 *result = nullptr;
-    if (int st = rt::enqueue_denoise(r, alpha, nullptr, s, &result)) return st;
-    RT_CK(cudaEventRecord(r->events.ev[EV_DENOISE1], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[2], s));
-    if (int st = rt::enqueue_resolve(r, result, alpha, nullptr, s)) return st;
-    RT_CK(cudaEventRecord(r->events.ev[EV_RESOLVE1], s));
-    if (fe[3]) RT_CK(cudaEventRecord(fe[3], s));
-    r->frames += 1;
-    r->have_frame_timing = true;
-    return RT_OK;
+    return rt::guarded("rt_render_frame", [&]() -> int {
+        if (int st = check_renderer(r, "rt_render_frame")) return st;
+        rt::clear_error();
+        cudaStream_t s = r->stream;
+        const rt_render_config &c = r->cfg;
+        const float alpha = rt::prepare_frame(r);
+        const uint32_t iters = rt::frame_iterations(r);
+        const size_t npix = (size_t)c.width * c.height;
+        if (npix > r->path.slots || sizeof(uint32_t) * 4 * ((size_t)iters + 1) > r->path.counts_bytes) {
+            RT_CK(cudaStreamSynchronize(s));
+            RT_CK(r->path.ensure(npix, iters));
+        }
+        cudaEvent_t fe[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (auto &e : fe) RT_CK(r->ring.next(&e));
+        RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
+        if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
+        const rtd::DevJob job = rt::make_job(r, 0u);
+        RT_CK(r->jobs.upload(&job, 1, s));
+        const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
+        const rtd::JobShape shape{c.width,
+                                  c.height,
+                                  (uint32_t)npix,
+                                  0u,
+                                  r->scene.stack_cap,
+                                  c.enable_photon_map ? 1u : 0u,
+                                  c.debug_view != 0u ? 1u : 0u,
+                                  r->scene.wnodes ? 1u : 0u,
+                                  r->scene.wide_stack};
+        if (r->prof_flags) {
+            if (int st = rt::profiled_gather(r, wp, shape, iters)) return st;
+        } else {
+            RT_CK(rtd::launch_wavefront(wp, &shape, 1u, iters, r->num_sms, r->tuning, s));
+        }
+        RT_CK(cudaEventRecord(r->events.ev[EV_GATHER1], s));
+        if (fe[3]) RT_CK(cudaEventRecord(fe[1], s));
+        float4 *result = nullptr;
+        if (int st = rt::enqueue_denoise(r, alpha, nullptr, s, &result)) return st;
+        RT_CK(cudaEventRecord(r->events.ev[EV_DENOISE1], s));
+        if (fe[3]) RT_CK(cudaEventRecord(fe[2], s));
+        if (int st = rt::enqueue_resolve(r, result, alpha, nullptr, s)) return st;
+        RT_CK(cudaEventRecord(r->events.ev[EV_RESOLVE1], s));
+        if (fe[3]) RT_CK(cudaEventRecord(fe[3], s));
+        r->frames += 1;
+        r->have_frame_timing = true;
+        return RT_OK;
+    });
 }
 
 namespace rt {
@@ -641,75 +651,89 @@ int profiled_gather(rt_renderer *r, rtd::WaveParams wp, const rtd::JobShape &sha
 }  // namespace rt
 
 extern "C" int rt_set_profiling(rt_renderer *r, uint32_t flags) {
-    if (int st = check_renderer(r, "rt_set_profiling")) return st;
-    if (flags & ~(RT_PROFILE_EVENTS | RT_PROFILE_COUNT)) {
-        set_error("rt_set_profiling: unknown flags 0x%x", flags);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    r->prof_flags = flags;
-    return RT_OK;
+    return rt::guarded("rt_set_profiling", [&]() -> int {
+        if (int st = check_renderer(r, "rt_set_profiling")) return st;
+        if (flags & ~(RT_PROFILE_EVENTS | RT_PROFILE_COUNT)) {
+            set_error("rt_set_profiling: unknown flags 0x%x", flags);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        r->prof_flags = flags;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_read_profile(rt_renderer *r, rt_trace_profile *out) {
-    if (int st = check_renderer(r, "rt_read_profile")) return st;
-    if (!out) {
-        set_error("rt_read_profile: null out");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    RT_CK(cudaStreamSynchronize(r->stream));
-    *out = r->prof;
-    r->prof = rt_trace_profile{};
-    return RT_OK;
+    return rt::guarded("rt_read_profile", [&]() -> int {
+        if (int st = check_renderer(r, "rt_read_profile")) return st;
+        if (!out) {
+            set_error("rt_read_profile: null out");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        RT_CK(cudaStreamSynchronize(r->stream));
+        *out = r->prof;
+        r->prof = rt_trace_profile{};
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_render_frames(rt_renderer *r, uint32_t n) {
-    if (int st = check_renderer(r, "rt_render_frames")) return st;
-    for (uint32_t i = 0; i < n; ++i)
-        if (int st = rt_render_frame(r)) return st;
-    return RT_OK;
+    return rt::guarded("rt_render_frames", [&]() -> int {
+        if (int st = check_renderer(r, "rt_render_frames")) return st;
+        for (uint32_t i = 0; i < n; ++i)
+            if (int st = rt_render_frame(r)) return st;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_update_camera(rt_renderer *r, const rt_camera *cam) {
-    if (int st = check_renderer(r, "rt_update_camera")) return st;
-    if (!cam) {
-        set_error("rt_update_camera: null camera");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    rt_camera_to_uniform(cam, r->cfg.width, r->cfg.height, &r->cam);
-    return RT_OK;
+    return rt::guarded("rt_update_camera", [&]() -> int {
+        if (int st = check_renderer(r, "rt_update_camera")) return st;
+        if (!cam) {
+            set_error("rt_update_camera: null camera");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        rt_camera_to_uniform(cam, r->cfg.width, r->cfg.height, &r->cam);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_update_camera_uniform(rt_renderer *r, const rt_camera_uniform *u) {
-    if (int st = check_renderer(r, "rt_update_camera_uniform")) return st;
-    if (!u) {
-        set_error("rt_update_camera_uniform: null uniform");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    r->cam = *u;
-    return RT_OK;
+    return rt::guarded("rt_update_camera_uniform", [&]() -> int {
+        if (int st = check_renderer(r, "rt_update_camera_uniform")) return st;
+        if (!u) {
+            set_error("rt_update_camera_uniform: null uniform");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        r->cam = *u;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_update_lights(rt_renderer *r, const rt_light *lights, uint64_t n) {
-    if (int st = check_renderer(r, "rt_update_lights")) return st;
-    if (n > r->lights_host.size() || (n && !lights)) {
-        set_error("rt_update_lights: %llu lights given, the light buffer holds %llu", (unsigned long long)n,
-                  (unsigned long long)r->lights_host.size());
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (n == 0) return RT_OK;
-    std::memcpy(r->lights_host.data(), lights, n * sizeof(rt_light));
-    RT_CK(cudaMemcpyAsync(r->d_lights.p, r->lights_host.data(), n * sizeof(rt_light), cudaMemcpyHostToDevice,
-                          r->stream));
-    RT_CK(cudaStreamSynchronize(r->stream));
-    resolve_env(r);
-    return RT_OK;
+    return rt::guarded("rt_update_lights", [&]() -> int {
+        if (int st = check_renderer(r, "rt_update_lights")) return st;
+        if (n > r->lights_host.size() || (n && !lights)) {
+            set_error("rt_update_lights: %llu lights given, the light buffer holds %llu", (unsigned long long)n,
+                      (unsigned long long)r->lights_host.size());
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if (n == 0) return RT_OK;
+        std::memcpy(r->lights_host.data(), lights, n * sizeof(rt_light));
+        RT_CK(cudaMemcpyAsync(r->d_lights.p, r->lights_host.data(), n * sizeof(rt_light), cudaMemcpyHostToDevice,
+                              r->stream));
+        RT_CK(cudaStreamSynchronize(r->stream));
+        resolve_env(r);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_reset_accumulation(rt_renderer *r, int hard) {
-    if (int st = check_renderer(r, "rt_reset_accumulation")) return st;
-    if (hard) RT_CK(cudaMemsetAsync(r->d_accum.p, 0, (size_t)r->cfg.width * r->cfg.height * 16, r->stream));
-    r->frames_since_reset = 0;
-    return RT_OK;
+    return rt::guarded("rt_reset_accumulation", [&]() -> int {
+        if (int st = check_renderer(r, "rt_reset_accumulation")) return st;
+        if (hard) RT_CK(cudaMemsetAsync(r->d_accum.p, 0, (size_t)r->cfg.width * r->cfg.height * 16, r->stream));
+        r->frames_since_reset = 0;
+        return RT_OK;
+    });
 }
 
 // Slots visited by the count/scatter dispatches of lib.rs:916,951,1026: floor(6P/256) groups of 256.
@@ -776,153 +800,173 @@ int rt::enqueue_photon_rebuild(rt_renderer *r) {
 }
 
 extern "C" int rt_rebuild_photons(rt_renderer *r) {
-    if (int st = check_renderer(r, "rt_rebuild_photons")) return st;
-    if (int st = rt::enqueue_photon_rebuild(r)) return st;
-    RT_CK(cudaStreamSynchronize(r->stream));
-    return RT_OK;
+    return rt::guarded("rt_rebuild_photons", [&]() -> int {
+        if (int st = check_renderer(r, "rt_rebuild_photons")) return st;
+        if (int st = rt::enqueue_photon_rebuild(r)) return st;
+        RT_CK(cudaStreamSynchronize(r->stream));
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_load_photons_and_build_grid(rt_renderer *r, const rt_photon *photons, uint64_t n) {
-    if (int st = check_renderer(r, "rt_load_photons_and_build_grid")) return st;
-    if (!r->photon_buffers || n != r->photon_slots || !photons) {
-        set_error("rt_load_photons_and_build_grid: need enable_photon_map and exactly %llu photons",
-                  (unsigned long long)r->photon_slots);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    cudaStream_t s = r->stream;
-    RT_CK(cudaMemcpyAsync(r->d_photons.p, photons, n * 64, cudaMemcpyHostToDevice, s));
-    RT_CK(rtd::launch_photon_keys(r->d_photons.as<float4>(), n, r->gp, r->d_keys.as<uint32_t>(), s));
-    RT_CK(cudaEventRecord(r->events.ev[EV_TRACE0], s));
-    RT_CK(cudaEventRecord(r->events.ev[EV_TRACE1], s));
-    if (int st = build_grid(r)) return st;
-    RT_CK(cudaEventRecord(r->events.ev[EV_GRID1], s));
-    RT_CK(cudaStreamSynchronize(s));
-    r->have_photon_timing = true;
-    return RT_OK;
+    return rt::guarded("rt_load_photons_and_build_grid", [&]() -> int {
+        if (int st = check_renderer(r, "rt_load_photons_and_build_grid")) return st;
+        if (!r->photon_buffers || n != r->photon_slots || !photons) {
+            set_error("rt_load_photons_and_build_grid: need enable_photon_map and exactly %llu photons",
+                      (unsigned long long)r->photon_slots);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        cudaStream_t s = r->stream;
+        RT_CK(cudaMemcpyAsync(r->d_photons.p, photons, n * 64, cudaMemcpyHostToDevice, s));
+        RT_CK(rtd::launch_photon_keys(r->d_photons.as<float4>(), n, r->gp, r->d_keys.as<uint32_t>(), s));
+        RT_CK(cudaEventRecord(r->events.ev[EV_TRACE0], s));
+        RT_CK(cudaEventRecord(r->events.ev[EV_TRACE1], s));
+        if (int st = build_grid(r)) return st;
+        RT_CK(cudaEventRecord(r->events.ev[EV_GRID1], s));
+        RT_CK(cudaStreamSynchronize(s));
+        r->have_photon_timing = true;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_set_config(rt_renderer *r, const rt_render_config *c) {
-    if (int st = check_renderer(r, "rt_set_config")) return st;
-    if (!c) {
-        set_error("rt_set_config: null config");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const rt_render_config &o = r->cfg;
-    if (c->width != o.width || c->height != o.height || c->photon_count != o.photon_count ||
-        c->grid_max_dim != o.grid_max_dim || c->photon_radius_mode != o.photon_radius_mode) {
-        set_error("rt_set_config: width, height, photon_count, grid_max_dim and photon_radius_mode are fixed at create");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    r->cfg = *c;
-    return RT_OK;
+    return rt::guarded("rt_set_config", [&]() -> int {
+        if (int st = check_renderer(r, "rt_set_config")) return st;
+        if (!c) {
+            set_error("rt_set_config: null config");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const rt_render_config &o = r->cfg;
+        if (c->width != o.width || c->height != o.height || c->photon_count != o.photon_count ||
+            c->grid_max_dim != o.grid_max_dim || c->photon_radius_mode != o.photon_radius_mode) {
+            set_error("rt_set_config: width, height, photon_count, grid_max_dim and photon_radius_mode are fixed at create");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        r->cfg = *c;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_get_config(const rt_renderer *r, rt_render_config *c) {
-    if (int st = check_renderer(r, "rt_get_config")) return st;
-    if (!c) return RT_ERR_INVALID_ARGUMENT;
-    *c = r->cfg;
-    return RT_OK;
+    return rt::guarded("rt_get_config", [&]() -> int {
+        if (int st = check_renderer(r, "rt_get_config")) return st;
+        if (!c) return RT_ERR_INVALID_ARGUMENT;
+        *c = r->cfg;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_set_light_marker(rt_renderer *r, const float marker[4], float glow) {
-    if (int st = check_renderer(r, "rt_set_light_marker")) return st;
-    if (marker) std::memcpy(r->marker, marker, sizeof(r->marker));
-    else std::memset(r->marker, 0, sizeof(r->marker));
-    r->glow = glow;
-    return RT_OK;
+    return rt::guarded("rt_set_light_marker", [&]() -> int {
+        if (int st = check_renderer(r, "rt_set_light_marker")) return st;
+        if (marker) std::memcpy(r->marker, marker, sizeof(r->marker));
+        else std::memset(r->marker, 0, sizeof(r->marker));
+        r->glow = glow;
+        return RT_OK;
+    });
 }
 
 extern "C" uint32_t rt_sample_count(const rt_renderer *r) { return r ? r->sample_counter : 0u; }
 
 extern "C" int rt_get_frame_state(const rt_renderer *r, uint32_t *sample_counter, uint32_t *frames_since_reset) {
-    if (int st = check_renderer(r, "rt_get_frame_state")) return st;
-    if (sample_counter) *sample_counter = r->sample_counter;
-    if (frames_since_reset) *frames_since_reset = r->frames_since_reset;
-    return RT_OK;
+    return rt::guarded("rt_get_frame_state", [&]() -> int {
+        if (int st = check_renderer(r, "rt_get_frame_state")) return st;
+        if (sample_counter) *sample_counter = r->sample_counter;
+        if (frames_since_reset) *frames_since_reset = r->frames_since_reset;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_restore_accumulation(rt_renderer *r, const float *rgba, uint64_t n_floats, uint32_t sample_counter,
                                        uint32_t frames_since_reset) {
-    if (int st = check_renderer(r, "rt_restore_accumulation")) return st;
-    const uint64_t n = (uint64_t)r->cfg.width * r->cfg.height * 4;
-    if (!rgba || n_floats != n) {
-        set_error("rt_restore_accumulation: need %llu floats (W * H * 4), got %llu", (unsigned long long)n,
-                  (unsigned long long)n_floats);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    RT_CK(cudaMemcpyAsync(r->d_accum.p, rgba, n * sizeof(float), cudaMemcpyHostToDevice, r->stream));
-    RT_CK(cudaStreamSynchronize(r->stream));  // the caller's buffer is only read during the call
-    r->sample_counter = sample_counter;
-    r->frames_since_reset = frames_since_reset;
-    return RT_OK;
+    return rt::guarded("rt_restore_accumulation", [&]() -> int {
+        if (int st = check_renderer(r, "rt_restore_accumulation")) return st;
+        const uint64_t n = (uint64_t)r->cfg.width * r->cfg.height * 4;
+        if (!rgba || n_floats != n) {
+            set_error("rt_restore_accumulation: need %llu floats (W * H * 4), got %llu", (unsigned long long)n,
+                      (unsigned long long)n_floats);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        RT_CK(cudaMemcpyAsync(r->d_accum.p, rgba, n * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+        RT_CK(cudaStreamSynchronize(r->stream));  // the caller's buffer is only read during the call
+        r->sample_counter = sample_counter;
+        r->frames_since_reset = frames_since_reset;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_synchronize(rt_renderer *r) {
-    if (int st = check_renderer(r, "rt_synchronize")) return st;
-    RT_CK(cudaStreamSynchronize(r->stream));
-    return RT_OK;
+    return rt::guarded("rt_synchronize", [&]() -> int {
+        if (int st = check_renderer(r, "rt_synchronize")) return st;
+        RT_CK(cudaStreamSynchronize(r->stream));
+        return RT_OK;
+    });
 }
 
 extern "C" void *rt_renderer_stream(rt_renderer *r) { return r ? (void *)r->stream : nullptr; }
 
 extern "C" int rt_get_grid_params(const rt_renderer *r, rt_grid_params *out) {
-    if (int st = check_renderer(r, "rt_get_grid_params")) return st;
-    if (!out) return RT_ERR_INVALID_ARGUMENT;
-    *out = r->gp;
-    return RT_OK;
+    return rt::guarded("rt_get_grid_params", [&]() -> int {
+        if (int st = check_renderer(r, "rt_get_grid_params")) return st;
+        if (!out) return RT_ERR_INVALID_ARGUMENT;
+        *out = r->gp;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_get_stats(rt_renderer *r, rt_frame_stats *out) {
-    if (int st = check_renderer(r, "rt_get_stats")) return st;
-    if (!out) return RT_ERR_INVALID_ARGUMENT;
-    std::memset(out, 0, sizeof(*out));
-    RT_CK(cudaStreamSynchronize(r->stream));
-    unsigned long long ctr[2] = {0, 0};
-    RT_CK(cudaMemcpy(ctr, r->d_counters.p, 16, cudaMemcpyDeviceToHost));
-    uint32_t total = 0;
-    RT_CK(cudaMemcpy(&total, r->d_total.p, 4, cudaMemcpyDeviceToHost));
-    out->frames = r->frames;
-    out->segments = ctr[0];
-    out->shadow_rays = ctr[1];
-    out->photons_stored = total;
-    auto ms = [&](int a, int b) {
-        float v = 0.0f;
-        if (cudaEventElapsedTime(&v, r->events.ev[a], r->events.ev[b]) != cudaSuccess) {
-            cudaGetLastError();
-            return 0.0f;
+    return rt::guarded("rt_get_stats", [&]() -> int {
+        if (int st = check_renderer(r, "rt_get_stats")) return st;
+        if (!out) return RT_ERR_INVALID_ARGUMENT;
+        std::memset(out, 0, sizeof(*out));
+        RT_CK(cudaStreamSynchronize(r->stream));
+        unsigned long long ctr[2] = {0, 0};
+        RT_CK(cudaMemcpy(ctr, r->d_counters.p, 16, cudaMemcpyDeviceToHost));
+        uint32_t total = 0;
+        RT_CK(cudaMemcpy(&total, r->d_total.p, 4, cudaMemcpyDeviceToHost));
+        out->frames = r->frames;
+        out->segments = ctr[0];
+        out->shadow_rays = ctr[1];
+        out->photons_stored = total;
+        auto ms = [&](int a, int b) {
+            float v = 0.0f;
+            if (cudaEventElapsedTime(&v, r->events.ev[a], r->events.ev[b]) != cudaSuccess) {
+                cudaGetLastError();
+                return 0.0f;
+            }
+            return v;
+        };
+        if (r->have_frame_timing) {
+            out->ms_gather = ms(EV_FRAME0, EV_GATHER1);
+            out->ms_denoise = ms(EV_GATHER1, EV_DENOISE1);
+            out->ms_resolve = ms(EV_DENOISE1, EV_RESOLVE1);
+            out->ms_frame = ms(EV_FRAME0, EV_RESOLVE1);
         }
-        return v;
-    };
-    if (r->have_frame_timing) {
-        out->ms_gather = ms(EV_FRAME0, EV_GATHER1);
-        out->ms_denoise = ms(EV_GATHER1, EV_DENOISE1);
-        out->ms_resolve = ms(EV_DENOISE1, EV_RESOLVE1);
-        out->ms_frame = ms(EV_FRAME0, EV_RESOLVE1);
-    }
-    if (r->have_photon_timing) {
-        out->ms_photon_trace = ms(EV_TRACE0, EV_TRACE1);
-        out->ms_grid_build = ms(EV_TRACE1, EV_GRID1);
-    }
-    // Drain the per-frame ring: complete groups of four events.
-    auto el = [](cudaEvent_t a, cudaEvent_t b) {
-        float v = 0.0f;
-        if (cudaEventElapsedTime(&v, a, b) != cudaSuccess) {
-            cudaGetLastError();
-            return 0.0;
+        if (r->have_photon_timing) {
+            out->ms_photon_trace = ms(EV_TRACE0, EV_TRACE1);
+            out->ms_grid_build = ms(EV_TRACE1, EV_GRID1);
         }
-        return (double)v;
-    };
-    const size_t groups = r->ring.used / 4;
-    for (size_t g = 0; g < groups; ++g) {
-        cudaEvent_t *e = &r->ring.pool[4 * g];
-        out->ms_gather_sum += el(e[0], e[1]);
-        out->ms_denoise_sum += el(e[1], e[2]);
-        out->ms_resolve_sum += el(e[2], e[3]);
-        out->ms_frame_sum += el(e[0], e[3]);
-    }
-    out->timed_frames = groups;
-    r->ring.used = 0;
-    return RT_OK;
+        // Drain the per-frame ring: complete groups of four events.
+        auto el = [](cudaEvent_t a, cudaEvent_t b) {
+            float v = 0.0f;
+            if (cudaEventElapsedTime(&v, a, b) != cudaSuccess) {
+                cudaGetLastError();
+                return 0.0;
+            }
+            return (double)v;
+        };
+        const size_t groups = r->ring.used / 4;
+        for (size_t g = 0; g < groups; ++g) {
+            cudaEvent_t *e = &r->ring.pool[4 * g];
+            out->ms_gather_sum += el(e[0], e[1]);
+            out->ms_denoise_sum += el(e[1], e[2]);
+            out->ms_resolve_sum += el(e[2], e[3]);
+            out->ms_frame_sum += el(e[0], e[3]);
+        }
+        out->timed_frames = groups;
+        r->ring.used = 0;
+        return RT_OK;
+    });
 }
 
 namespace {
@@ -941,57 +985,73 @@ int read_back(rt_renderer *r, const DevBuf &b, void *dst, uint64_t bytes, uint64
 
 #define RT_IMG_BYTES(r) ((uint64_t)(r)->cfg.width * (r)->cfg.height * 16)
 extern "C" int rt_read_accumulation(rt_renderer *r, float *rgba, uint64_t n) {
-    return r ? read_back(r, r->d_accum, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_accumulation")
-             : check_renderer(r, "rt_read_accumulation");
+    return rt::guarded("rt_read_accumulation", [&]() -> int {
+        return r ? read_back(r, r->d_accum, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_accumulation")
+                 : check_renderer(r, "rt_read_accumulation");
+    });
 }
 extern "C" int rt_read_frame(rt_renderer *r, float *rgba, uint64_t n) {
-    if (!r) return check_renderer(r, "rt_read_frame");
-    // The frame as composite consumed it (after the denoise passes, if any).
-    const DevBuf &b = (r->last_denoise_passes % 2 == 1) ? r->d_pingpong : r->d_frame;
-    return read_back(r, b, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_frame");
+    return rt::guarded("rt_read_frame", [&]() -> int {
+        if (!r) return check_renderer(r, "rt_read_frame");
+        // The frame as composite consumed it (after the denoise passes, if any).
+        const DevBuf &b = (r->last_denoise_passes % 2 == 1) ? r->d_pingpong : r->d_frame;
+        return read_back(r, b, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_frame");
+    });
 }
 extern "C" int rt_read_moments(rt_renderer *r, float *rgba, uint64_t n) {
-    return r ? read_back(r, r->d_moments, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_moments")
-             : check_renderer(r, "rt_read_moments");
+    return rt::guarded("rt_read_moments", [&]() -> int {
+        return r ? read_back(r, r->d_moments, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_moments")
+                 : check_renderer(r, "rt_read_moments");
+    });
 }
 extern "C" int rt_read_gbuffer(rt_renderer *r, float *rgba, uint64_t n) {
-    return r ? read_back(r, r->d_gbuffer, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_gbuffer")
-             : check_renderer(r, "rt_read_gbuffer");
+    return rt::guarded("rt_read_gbuffer", [&]() -> int {
+        return r ? read_back(r, r->d_gbuffer, rgba, n * 4, RT_IMG_BYTES(r), "rt_read_gbuffer")
+                 : check_renderer(r, "rt_read_gbuffer");
+    });
 }
 extern "C" int rt_read_tonemapped(rt_renderer *r, uint8_t *rgba8, uint64_t n) {
-    return r ? read_back(r, r->d_output, rgba8, n, RT_IMG_BYTES(r) / 4, "rt_read_tonemapped")
-             : check_renderer(r, "rt_read_tonemapped");
+    return rt::guarded("rt_read_tonemapped", [&]() -> int {
+        return r ? read_back(r, r->d_output, rgba8, n, RT_IMG_BYTES(r) / 4, "rt_read_tonemapped")
+                 : check_renderer(r, "rt_read_tonemapped");
+    });
 }
 extern "C" int rt_read_photons(rt_renderer *r, rt_photon *out, uint64_t n) {
-    return r ? read_back(r, r->d_photons, out, n * 64, r->photon_slots * 64, "rt_read_photons")
-             : check_renderer(r, "rt_read_photons");
+    return rt::guarded("rt_read_photons", [&]() -> int {
+        return r ? read_back(r, r->d_photons, out, n * 64, r->photon_slots * 64, "rt_read_photons")
+                 : check_renderer(r, "rt_read_photons");
+    });
 }
 extern "C" int rt_read_sorted_photons(rt_renderer *r, rt_photon *out, uint64_t n) {
-    return r ? read_back(r, r->d_sorted, out, n * 64, r->photon_slots * 64, "rt_read_sorted_photons")
-             : check_renderer(r, "rt_read_sorted_photons");
+    return rt::guarded("rt_read_sorted_photons", [&]() -> int {
+        return r ? read_back(r, r->d_sorted, out, n * 64, r->photon_slots * 64, "rt_read_sorted_photons")
+                 : check_renderer(r, "rt_read_sorted_photons");
+    });
 }
 extern "C" int rt_read_photon_grid(rt_renderer *r, uint32_t *counts, uint32_t *meta, uint64_t num_cells) {
-    if (int st = check_renderer(r, "rt_read_photon_grid")) return st;
-    if (num_cells < r->gp.num_cells) {
-        set_error("rt_read_photon_grid: %llu cells given, the grid has %u", (unsigned long long)num_cells,
-                  r->gp.num_cells);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    // The build turns the per-cell counts into (start, count) pairs and clears them for the next
-    // build, so the counts are read from the pairs.
-    const uint64_t C = r->gp.num_cells;
-    std::vector<uint32_t> pairs;
-    uint32_t *m = meta;
-    if (!m && counts) {
-        pairs.resize(2 * C);
-        m = pairs.data();
-    }
-    if (m) {
-        if (int st = read_back(r, r->d_meta, m, (meta ? num_cells : C) * 8, C * 8, "rt_read_photon_grid")) return st;
-    }
-    if (counts)
-        for (uint64_t c = 0; c < C; ++c) counts[c] = m[2 * c + 1];
-    return RT_OK;
+    return rt::guarded("rt_read_photon_grid", [&]() -> int {
+        if (int st = check_renderer(r, "rt_read_photon_grid")) return st;
+        if (num_cells < r->gp.num_cells) {
+            set_error("rt_read_photon_grid: %llu cells given, the grid has %u", (unsigned long long)num_cells,
+                      r->gp.num_cells);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        // The build turns the per-cell counts into (start, count) pairs and clears them for the next
+        // build, so the counts are read from the pairs.
+        const uint64_t C = r->gp.num_cells;
+        std::vector<uint32_t> pairs;
+        uint32_t *m = meta;
+        if (!m && counts) {
+            pairs.resize(2 * C);
+            m = pairs.data();
+        }
+        if (m) {
+            if (int st = read_back(r, r->d_meta, m, (meta ? num_cells : C) * 8, C * 8, "rt_read_photon_grid")) return st;
+        }
+        if (counts)
+            for (uint64_t c = 0; c < C; ++c) counts[c] = m[2 * c + 1];
+        return RT_OK;
+    });
 }
 
 // ================================================================================================
@@ -999,109 +1059,115 @@ extern "C" int rt_read_photon_grid(rt_renderer *r, uint32_t *counts, uint32_t *m
 // ================================================================================================
 extern "C" int rt_stage_denoise(const float *frame_rgba, const float *gbuffer, const float *moments, uint32_t width,
                                 uint32_t height, float alpha, uint32_t passes, float *out_rgba) {
-    rt::clear_error();
-    if (!frame_rgba || !gbuffer || !moments || !out_rgba || !width || !height) {
-        set_error("rt_stage_denoise: invalid arguments");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const size_t bytes = (size_t)width * height * 16;
-    DevBuf a, b, g, m;
-    RT_CK(a.alloc(bytes));
-    RT_CK(b.alloc(bytes));
-    RT_CK(g.alloc(bytes));
-    RT_CK(m.alloc(bytes));
-    RT_CK(cudaMemcpy(a.p, frame_rgba, bytes, cudaMemcpyHostToDevice));
-    RT_CK(cudaMemcpy(g.p, gbuffer, bytes, cudaMemcpyHostToDevice));
-    RT_CK(cudaMemcpy(m.p, moments, bytes, cudaMemcpyHostToDevice));
-    float4 *cur = a.as<float4>(), *nxt = b.as<float4>();
-    for (uint32_t it = 0; it < passes; ++it) {
-        rt_denoise_params dp;
-        std::memset(&dp, 0, sizeof(dp));
-        dp.width = width;
-        dp.height = height;
-        dp.step_size = 1u << it;
-        dp.lambda = 3.0f;
-        dp.phi_normal = 12.0f;
-        dp.phi_depth = 0.05f;
-        dp.alpha = alpha;
-        RT_CK(rtd::launch_denoise(cur, nxt, g.as<float4>(), m.as<float4>(), dp, nullptr, 0));
-        std::swap(cur, nxt);
-    }
-    RT_CK(cudaMemcpy(out_rgba, cur, bytes, cudaMemcpyDeviceToHost));
-    return RT_OK;
+    return rt::guarded("rt_stage_denoise", [&]() -> int {
+        rt::clear_error();
+        if (!frame_rgba || !gbuffer || !moments || !out_rgba || !width || !height) {
+            set_error("rt_stage_denoise: invalid arguments");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const size_t bytes = (size_t)width * height * 16;
+        DevBuf a, b, g, m;
+        RT_CK(a.alloc(bytes));
+        RT_CK(b.alloc(bytes));
+        RT_CK(g.alloc(bytes));
+        RT_CK(m.alloc(bytes));
+        RT_CK(cudaMemcpy(a.p, frame_rgba, bytes, cudaMemcpyHostToDevice));
+        RT_CK(cudaMemcpy(g.p, gbuffer, bytes, cudaMemcpyHostToDevice));
+        RT_CK(cudaMemcpy(m.p, moments, bytes, cudaMemcpyHostToDevice));
+        float4 *cur = a.as<float4>(), *nxt = b.as<float4>();
+        for (uint32_t it = 0; it < passes; ++it) {
+            rt_denoise_params dp;
+            std::memset(&dp, 0, sizeof(dp));
+            dp.width = width;
+            dp.height = height;
+            dp.step_size = 1u << it;
+            dp.lambda = 3.0f;
+            dp.phi_normal = 12.0f;
+            dp.phi_depth = 0.05f;
+            dp.alpha = alpha;
+            RT_CK(rtd::launch_denoise(cur, nxt, g.as<float4>(), m.as<float4>(), dp, nullptr, 0));
+            std::swap(cur, nxt);
+        }
+        RT_CK(cudaMemcpy(out_rgba, cur, bytes, cudaMemcpyDeviceToHost));
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_stage_resolve(const float *frame_rgba, float *accum_inout, const float *gbuffer, uint32_t width,
                                 uint32_t height, float alpha, const rt_tonemap_params *tp, uint8_t *out_rgba8) {
-    rt::clear_error();
-    if (!frame_rgba || !accum_inout || !tp || !out_rgba8 || !width || !height) {
-        set_error("rt_stage_resolve: invalid arguments");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const size_t bytes = (size_t)width * height * 16;
-    DevBuf f, a, g, o;
-    RT_CK(f.alloc(bytes));
-    RT_CK(a.alloc(bytes));
-    RT_CK(o.alloc(bytes / 4));
-    RT_CK(cudaMemcpy(f.p, frame_rgba, bytes, cudaMemcpyHostToDevice));
-    RT_CK(cudaMemcpy(a.p, accum_inout, bytes, cudaMemcpyHostToDevice));
-    const float4 *gp = nullptr;
-    if (gbuffer) {
-        RT_CK(g.alloc(bytes));
-        RT_CK(cudaMemcpy(g.p, gbuffer, bytes, cudaMemcpyHostToDevice));
-        gp = g.as<float4>();
-    }
-    rt_tonemap_params t = *tp;
-    t.width = width;
-    RT_CK(rtd::launch_resolve(f.as<float4>(), a.as<float4>(), gp, width, height, alpha, nullptr, t, o.as<uchar4>(), 0));
-    RT_CK(cudaMemcpy(accum_inout, a.p, bytes, cudaMemcpyDeviceToHost));
-    RT_CK(cudaMemcpy(out_rgba8, o.p, bytes / 4, cudaMemcpyDeviceToHost));
-    return RT_OK;
+    return rt::guarded("rt_stage_resolve", [&]() -> int {
+        rt::clear_error();
+        if (!frame_rgba || !accum_inout || !tp || !out_rgba8 || !width || !height) {
+            set_error("rt_stage_resolve: invalid arguments");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const size_t bytes = (size_t)width * height * 16;
+        DevBuf f, a, g, o;
+        RT_CK(f.alloc(bytes));
+        RT_CK(a.alloc(bytes));
+        RT_CK(o.alloc(bytes / 4));
+        RT_CK(cudaMemcpy(f.p, frame_rgba, bytes, cudaMemcpyHostToDevice));
+        RT_CK(cudaMemcpy(a.p, accum_inout, bytes, cudaMemcpyHostToDevice));
+        const float4 *gp = nullptr;
+        if (gbuffer) {
+            RT_CK(g.alloc(bytes));
+            RT_CK(cudaMemcpy(g.p, gbuffer, bytes, cudaMemcpyHostToDevice));
+            gp = g.as<float4>();
+        }
+        rt_tonemap_params t = *tp;
+        t.width = width;
+        RT_CK(rtd::launch_resolve(f.as<float4>(), a.as<float4>(), gp, width, height, alpha, nullptr, t, o.as<uchar4>(), 0));
+        RT_CK(cudaMemcpy(accum_inout, a.p, bytes, cudaMemcpyDeviceToHost));
+        RT_CK(cudaMemcpy(out_rgba8, o.p, bytes / 4, cudaMemcpyDeviceToHost));
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_stage_photon_grid(const rt_photon *photons, const rt_grid_params *gpp, uint32_t *counts,
                                     uint32_t *meta, rt_photon *sorted) {
-    rt::clear_error();
-    if (!photons || !gpp || !counts || !meta || !sorted || gpp->num_cells == 0) {
-        set_error("rt_stage_photon_grid: invalid arguments");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const rt_grid_params gp = *gpp;
-    const uint64_t S = gp.photon_slots, C = gp.num_cells;
-    DevBuf ph, keys, rank, order, srt, cnt, cur, mt, part, tot;
-    RT_CK(ph.alloc(S * 64));
-    RT_CK(keys.alloc(S * 4));
-    RT_CK(rank.alloc(S * 4));
-    RT_CK(order.alloc(S * 4));
-    RT_CK(srt.alloc(S * 64));
-    RT_CK(cnt.alloc(C * 4));
-    RT_CK(cur.alloc(C * 4));
-    RT_CK(mt.alloc(C * 8));
-    RT_CK(part.alloc((size_t)rtd::grid_scan_partials((uint32_t)C) * 4));
-    RT_CK(tot.alloc(16));
-    if (S) RT_CK(cudaMemcpy(ph.p, photons, S * 64, cudaMemcpyHostToDevice));
-    RT_CK(cudaMemset(srt.p, 0, S * 64 ? S * 64 : 16));
-    RT_CK(cudaMemset(tot.p, 0, 16));
-    RT_CK(cudaMemset(cnt.p, 0, C * 4));  // the build expects zero counts and leaves them zero
-    RT_CK(rtd::launch_photon_keys(ph.as<float4>(), S, gp, keys.as<uint32_t>(), 0));
-    rtd::GridBuffers g;
-    g.photons = ph.as<float4>();
-    g.keys = keys.as<uint32_t>();
-    g.slot_count = S;
-    g.num_cells = (uint32_t)C;
-    g.counts = cnt.as<uint32_t>();
-    g.meta = mt.as<uint2>();
-    g.cursor = cur.as<uint32_t>();
-    g.order = order.as<uint32_t>();
-    g.sorted = srt.as<float4>();
-    g.sorted_pos = nullptr;
-    g.scan_partials = part.as<uint32_t>();
-    g.total = tot.as<uint32_t>();
-    g.rank = rank.as<uint32_t>();
-    RT_CK(rtd::launch_grid_build(g, 0));
-    RT_CK(cudaMemcpy(meta, mt.p, C * 8, cudaMemcpyDeviceToHost));
-    for (uint64_t c = 0; c < C; ++c) counts[c] = meta[2 * c + 1];  // the build cleared the counts
-    if (S) RT_CK(cudaMemcpy(sorted, srt.p, S * 64, cudaMemcpyDeviceToHost));
-    return RT_OK;
+    return rt::guarded("rt_stage_photon_grid", [&]() -> int {
+        rt::clear_error();
+        if (!photons || !gpp || !counts || !meta || !sorted || gpp->num_cells == 0) {
+            set_error("rt_stage_photon_grid: invalid arguments");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const rt_grid_params gp = *gpp;
+        const uint64_t S = gp.photon_slots, C = gp.num_cells;
+        DevBuf ph, keys, rank, order, srt, cnt, cur, mt, part, tot;
+        RT_CK(ph.alloc(S * 64));
+        RT_CK(keys.alloc(S * 4));
+        RT_CK(rank.alloc(S * 4));
+        RT_CK(order.alloc(S * 4));
+        RT_CK(srt.alloc(S * 64));
+        RT_CK(cnt.alloc(C * 4));
+        RT_CK(cur.alloc(C * 4));
+        RT_CK(mt.alloc(C * 8));
+        RT_CK(part.alloc((size_t)rtd::grid_scan_partials((uint32_t)C) * 4));
+        RT_CK(tot.alloc(16));
+        if (S) RT_CK(cudaMemcpy(ph.p, photons, S * 64, cudaMemcpyHostToDevice));
+        RT_CK(cudaMemset(srt.p, 0, S * 64 ? S * 64 : 16));
+        RT_CK(cudaMemset(tot.p, 0, 16));
+        RT_CK(cudaMemset(cnt.p, 0, C * 4));  // the build expects zero counts and leaves them zero
+        RT_CK(rtd::launch_photon_keys(ph.as<float4>(), S, gp, keys.as<uint32_t>(), 0));
+        rtd::GridBuffers g;
+        g.photons = ph.as<float4>();
+        g.keys = keys.as<uint32_t>();
+        g.slot_count = S;
+        g.num_cells = (uint32_t)C;
+        g.counts = cnt.as<uint32_t>();
+        g.meta = mt.as<uint2>();
+        g.cursor = cur.as<uint32_t>();
+        g.order = order.as<uint32_t>();
+        g.sorted = srt.as<float4>();
+        g.sorted_pos = nullptr;
+        g.scan_partials = part.as<uint32_t>();
+        g.total = tot.as<uint32_t>();
+        g.rank = rank.as<uint32_t>();
+        RT_CK(rtd::launch_grid_build(g, 0));
+        RT_CK(cudaMemcpy(meta, mt.p, C * 8, cudaMemcpyDeviceToHost));
+        for (uint64_t c = 0; c < C; ++c) counts[c] = meta[2 * c + 1];  // the build cleared the counts
+        if (S) RT_CK(cudaMemcpy(sorted, srt.p, S * 64, cudaMemcpyDeviceToHost));
+        return RT_OK;
+    });
 }
 

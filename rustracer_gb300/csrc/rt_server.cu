@@ -88,6 +88,9 @@ struct rt_server {
     std::map<uint32_t, SceneEntry> scenes;                   // entries added under mu before any submit uses them
     uint64_t next_id = 1;
     bool stop = false;
+    // Set (under mu) when the worker thread ran out of host memory: later submits are refused.
+    bool broken = false;
+    std::string broken_msg;
     rt_server_stats st{};                                    // under mu
     // worker-only state
     std::vector<Job *> active;
@@ -344,8 +347,7 @@ bool launch(rt_server *s) {
     return true;
 }
 
-void worker_main(rt_server *s) {
-    cudaSetDevice(s->device);
+void worker_loop(rt_server *s) {
     for (;;) {
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -377,59 +379,103 @@ void worker_main(rt_server *s) {
     }
 }
 
+// After the worker loop threw: waits for the frames in flight and fails every job not yet done, so
+// that rt_server_wait_idle returns and each job's status says why.
+void fail_everything(rt_server *s, const char *why) {
+    for (Flight &f : s->flights) cudaEventSynchronize(f.ev);
+    for (Flight &f : s->flights) cudaEventDestroy(f.ev);
+    s->flights.clear();
+    for (Job *j : std::vector<Job *>(s->active)) {
+        fail_job(s, j, why);
+        retire(s, j, false);
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Job *j : s->pending) {
+        j->state = RT_JOB_FAILED;
+        j->error = why;
+        j->t_done = s->now_ms();
+        s->st.failed += 1;
+    }
+    s->pending.clear();
+}
+
+void worker_main(rt_server *s) {
+    cudaSetDevice(s->device);
+    try {
+        worker_loop(s);
+        return;
+    } catch (const std::exception &e) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->broken = true;
+        s->broken_msg = std::string("server worker stopped: ") + e.what();
+    }
+    try {
+        fail_everything(s, s->broken_msg.c_str());
+    } catch (const std::exception &) {
+        // nothing more can be freed without host memory; destroy releases the rest
+    }
+}
+
 }  // namespace
 
 extern "C" int rt_server_create(const rt_server_config *cfg, rt_server **out) {
-    rt::clear_error();
-    if (!out) {
-        set_error("rt_server_create: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    if (rt_device_count() <= 0) {
-        set_error("rt_server_create: no CUDA device is visible");
-        return RT_ERR_CUDA;
-    }
-    rt_server *s = new (std::nothrow) rt_server();
-    if (!s) {
-        set_error("rt_server_create: out of host memory");
-        return RT_ERR_OUT_OF_MEMORY;
-    }
-    if (cfg) s->cfg = *cfg;
-    if (s->cfg.mode > RT_SERVER_PLAIN) {
-        delete s;
-        set_error("rt_server_create: mode must be RT_SERVER_BATCHED or RT_SERVER_PLAIN");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (!s->cfg.hbm_cap_bytes) s->cfg.hbm_cap_bytes = 120ull << 30;
-    if (!s->cfg.max_jobs) s->cfg.max_jobs = 64;
-    if (!s->cfg.max_slots) s->cfg.max_slots = 1u << 25;
-    if (!s->cfg.frames_in_flight) s->cfg.frames_in_flight = 2;
-    cudaGetDevice(&s->device);
-    s->t0 = Clock::now();
-    if (s->plain()) {
-        s->cfg.max_jobs = 1;
-        s->cfg.graphs = 0;
-    }
-    const rt::GraphMode gm = s->cfg.graphs ? rt::GraphMode::OnRepeat : rt::GraphMode::Off;
-    int st = s->eng.init(s->cfg.max_jobs, gm);
-    const rt_wavefront_tuning &tc = s->cfg.tuning;
-    if (tc.block_threads | tc.blocks_per_sm | tc.chunk | tc.steps | tc.stack_entries) {
-        s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk,
-                                        tc.steps,         tc.stack_entries, tc.treelet ? rtd::kTreeletRecords : 0u,
-                                        tc.shade_blocks, tc.refill_idle};
-        rtd::normalize_tuning(s->eng.tuning, 0u);
-    }
-    if (st == RT_OK) st = s->eng.reserve(s->cfg.max_slots, 64);
-    if (st != RT_OK) {
-        delete s;
-        return st;
-    }
-    s->path_bytes = rt::path_state_bytes(s->cfg.max_slots, 64);
-    charge_locked(s, (int64_t)s->path_bytes);
-    s->worker = std::thread(worker_main, s);
-    *out = s;
-    return RT_OK;
+    return rt::guarded("rt_server_create", [&]() -> int {
+        rt::clear_error();
+        if (!out) {
+            set_error("rt_server_create: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        *out = nullptr;
+        if (rt_device_count() <= 0) {
+            set_error("rt_server_create: no CUDA device is visible");
+            return RT_ERR_CUDA;
+        }
+        rt_server *s = new (std::nothrow) rt_server();
+        if (!s) {
+            set_error("rt_server_create: out of host memory");
+            return RT_ERR_OUT_OF_MEMORY;
+        }
+        if (cfg) s->cfg = *cfg;
+        if (s->cfg.mode > RT_SERVER_PLAIN) {
+            delete s;
+            set_error("rt_server_create: mode must be RT_SERVER_BATCHED or RT_SERVER_PLAIN");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if (!s->cfg.hbm_cap_bytes) s->cfg.hbm_cap_bytes = 120ull << 30;
+        if (!s->cfg.max_jobs) s->cfg.max_jobs = 64;
+        if (!s->cfg.max_slots) s->cfg.max_slots = 1u << 25;
+        if (!s->cfg.frames_in_flight) s->cfg.frames_in_flight = 2;
+        cudaGetDevice(&s->device);
+        s->t0 = Clock::now();
+        if (s->plain()) {
+            s->cfg.max_jobs = 1;
+            s->cfg.graphs = 0;
+        }
+        const rt::GraphMode gm = s->cfg.graphs ? rt::GraphMode::OnRepeat : rt::GraphMode::Off;
+        int st = s->eng.init(s->cfg.max_jobs, gm);
+        const rt_wavefront_tuning &tc = s->cfg.tuning;
+        if (tc.block_threads | tc.blocks_per_sm | tc.chunk | tc.steps | tc.stack_entries) {
+            s->eng.tuning = rtd::WaveTuning{tc.block_threads, tc.blocks_per_sm, tc.chunk,
+                                            tc.steps,         tc.stack_entries, tc.treelet ? rtd::kTreeletRecords : 0u,
+                                            tc.shade_blocks, tc.refill_idle};
+            rtd::normalize_tuning(s->eng.tuning, 0u);
+        }
+        if (st == RT_OK) st = s->eng.reserve(s->cfg.max_slots, 64);
+        if (st != RT_OK) {
+            delete s;
+            return st;
+        }
+        s->path_bytes = rt::path_state_bytes(s->cfg.max_slots, 64);
+        charge_locked(s, (int64_t)s->path_bytes);
+        try {
+            s->worker = std::thread(worker_main, s);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = s;
+        return RT_OK;
+    });
 }
 
 extern "C" void rt_server_destroy(rt_server *s) {
@@ -449,174 +495,198 @@ extern "C" void rt_server_destroy(rt_server *s) {
 }
 
 extern "C" int rt_server_add_scene(rt_server *s, uint32_t scene_id, const rt_scene_desc *desc) {
-    rt::clear_error();
-    if (!s || !desc) {
-        set_error("rt_server_add_scene: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if ((desc->triangle_count && !desc->triangles) || (desc->bvh_node_count && !desc->bvh_nodes) ||
-        (desc->bvh_prim_count && !desc->bvh_prims) || (desc->material_count && !desc->materials) ||
-        (desc->light_count && !desc->lights)) {
-        set_error("rt_server_add_scene: scene array pointer is null with a non-zero count");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->scenes.count(scene_id)) {
-        set_error("rt_server_add_scene: scene %u is already registered", scene_id);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    SceneEntry &e = s->scenes[scene_id];
-    e.desc = *desc;
-    e.bytes = scene_estimate(*desc);
-    return RT_OK;
+    return rt::guarded("rt_server_add_scene", [&]() -> int {
+        rt::clear_error();
+        if (!s || !desc) {
+            set_error("rt_server_add_scene: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if ((desc->triangle_count && !desc->triangles) || (desc->bvh_node_count && !desc->bvh_nodes) ||
+            (desc->bvh_prim_count && !desc->bvh_prims) || (desc->material_count && !desc->materials) ||
+            (desc->light_count && !desc->lights)) {
+            set_error("rt_server_add_scene: scene array pointer is null with a non-zero count");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->scenes.count(scene_id)) {
+            set_error("rt_server_add_scene: scene %u is already registered", scene_id);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        SceneEntry &e = s->scenes[scene_id];
+        e.desc = *desc;
+        e.bytes = scene_estimate(*desc);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_server_submit(rt_server *s, const rt_request *req, uint64_t *job_id) {
-    rt::clear_error();
-    if (!s || !req) {
-        set_error("rt_server_submit: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const rt_render_config &c = req->config;
-    if (c.width == 0 || c.height == 0 || (uint64_t)c.width * c.height > (1ull << 28) || req->budget_frames == 0) {
-        set_error("rt_server_submit: width, height and budget_frames must be non-zero (width*height <= 2^28)");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (c.enable_photon_map && (uint64_t)c.photon_count * RT_MAX_BOUNCES > 0xFFFFFFFFull) {
-        set_error("rt_server_submit: photon_count * 6 must fit in 32 bits");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::unique_ptr<Job> j(new (std::nothrow) Job());
-    if (!j) {
-        set_error("rt_server_submit: out of host memory");
-        return RT_ERR_OUT_OF_MEMORY;
-    }
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        if (!s->scenes.count(req->scene_id)) {
-            set_error("rt_server_submit: scene %u is not registered", req->scene_id);
+    return rt::guarded("rt_server_submit", [&]() -> int {
+        rt::clear_error();
+        if (!s || !req) {
+            set_error("rt_server_submit: null argument");
             return RT_ERR_INVALID_ARGUMENT;
         }
-        j->id = s->next_id++;
-        j->req = *req;
-        j->npix = (uint64_t)c.width * c.height;
-        j->t_submit = s->now_ms();
-        if (job_id) *job_id = j->id;
-        s->pending.push_back(j.get());
-        s->jobs[j->id] = std::move(j);
-        s->st.submitted += 1;
-        s->st.pending = (uint32_t)s->pending.size();
-    }
-    s->cv.notify_all();
-    return RT_OK;
+        const rt_render_config &c = req->config;
+        if (c.width == 0 || c.height == 0 || (uint64_t)c.width * c.height > (1ull << 28) || req->budget_frames == 0) {
+            set_error("rt_server_submit: width, height and budget_frames must be non-zero (width*height <= 2^28)");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if (c.enable_photon_map && (uint64_t)c.photon_count * RT_MAX_BOUNCES > 0xFFFFFFFFull) {
+            set_error("rt_server_submit: photon_count * 6 must fit in 32 bits");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::unique_ptr<Job> j(new (std::nothrow) Job());
+        if (!j) {
+            set_error("rt_server_submit: out of host memory");
+            return RT_ERR_OUT_OF_MEMORY;
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (s->broken) {
+                set_error("rt_server_submit: %s", s->broken_msg.c_str());
+                return RT_ERR_STATE;
+            }
+            if (!s->scenes.count(req->scene_id)) {
+                set_error("rt_server_submit: scene %u is not registered", req->scene_id);
+                return RT_ERR_INVALID_ARGUMENT;
+            }
+            Job *raw = j.get();
+            raw->id = s->next_id++;
+            raw->req = *req;
+            raw->npix = (uint64_t)c.width * c.height;
+            raw->t_submit = s->now_ms();
+            s->jobs.emplace(raw->id, std::move(j));
+            try {
+                s->pending.push_back(raw);
+            } catch (...) {
+                s->jobs.erase(raw->id);
+                throw;
+            }
+            if (job_id) *job_id = raw->id;
+            s->st.submitted += 1;
+            s->st.pending = (uint32_t)s->pending.size();
+        }
+        s->cv.notify_all();
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_server_job_status(rt_server *s, uint64_t job_id, rt_job_status *out) {
-    if (!s || !out) {
-        set_error("rt_server_job_status: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->jobs.find(job_id);
-    if (it == s->jobs.end()) {
-        set_error("rt_server_job_status: no job %llu", (unsigned long long)job_id);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const Job &j = *it->second;
-    std::memset(out, 0, sizeof(*out));
-    out->job_id = j.id;
-    out->state = j.state;
-    out->frames_done = j.done;
-    out->t_submit_ms = j.t_submit;
-    out->t_admit_ms = j.t_admit;
-    out->t_first_frame_ms = j.t_first;
-    out->t_done_ms = j.t_done;
-    return RT_OK;
+    return rt::guarded("rt_server_job_status", [&]() -> int {
+        if (!s || !out) {
+            set_error("rt_server_job_status: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) {
+            set_error("rt_server_job_status: no job %llu", (unsigned long long)job_id);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const Job &j = *it->second;
+        std::memset(out, 0, sizeof(*out));
+        out->job_id = j.id;
+        out->state = j.state;
+        out->frames_done = j.done;
+        out->t_submit_ms = j.t_submit;
+        out->t_admit_ms = j.t_admit;
+        out->t_first_frame_ms = j.t_first;
+        out->t_done_ms = j.t_done;
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_server_read_result(rt_server *s, uint64_t job_id, float *rgba, uint64_t n_floats) {
-    if (!s || !rgba) {
-        set_error("rt_server_read_result: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->jobs.find(job_id);
-    if (it == s->jobs.end()) {
-        set_error("rt_server_read_result: no job %llu", (unsigned long long)job_id);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const Job &j = *it->second;
-    if (j.state != RT_JOB_DONE || !j.req.keep_result) {
-        set_error("rt_server_read_result: job %llu is not done or was submitted without keep_result",
-                  (unsigned long long)job_id);
-        return RT_ERR_STATE;
-    }
-    if (n_floats != j.result.size()) {
-        set_error("rt_server_read_result: %llu floats given, the result has %llu", (unsigned long long)n_floats,
-                  (unsigned long long)j.result.size());
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::memcpy(rgba, j.result.data(), n_floats * sizeof(float));
-    return RT_OK;
+    return rt::guarded("rt_server_read_result", [&]() -> int {
+        if (!s || !rgba) {
+            set_error("rt_server_read_result: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) {
+            set_error("rt_server_read_result: no job %llu", (unsigned long long)job_id);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        const Job &j = *it->second;
+        if (j.state != RT_JOB_DONE || !j.req.keep_result) {
+            set_error("rt_server_read_result: job %llu is not done or was submitted without keep_result",
+                      (unsigned long long)job_id);
+            return RT_ERR_STATE;
+        }
+        if (n_floats != j.result.size()) {
+            set_error("rt_server_read_result: %llu floats given, the result has %llu", (unsigned long long)n_floats,
+                      (unsigned long long)j.result.size());
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::memcpy(rgba, j.result.data(), n_floats * sizeof(float));
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_server_release_job(rt_server *s, uint64_t job_id) {
-    if (!s) {
-        set_error("rt_server_release_job: null server");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->jobs.find(job_id);
-    if (it == s->jobs.end()) {
-        set_error("rt_server_release_job: no job %llu", (unsigned long long)job_id);
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    if (it->second->state != RT_JOB_DONE && it->second->state != RT_JOB_FAILED) {
-        set_error("rt_server_release_job: job %llu is still queued or running", (unsigned long long)job_id);
-        return RT_ERR_STATE;
-    }
-    s->jobs.erase(it);
-    return RT_OK;
+    return rt::guarded("rt_server_release_job", [&]() -> int {
+        if (!s) {
+            set_error("rt_server_release_job: null server");
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) {
+            set_error("rt_server_release_job: no job %llu", (unsigned long long)job_id);
+            return RT_ERR_INVALID_ARGUMENT;
+        }
+        if (it->second->state != RT_JOB_DONE && it->second->state != RT_JOB_FAILED) {
+            set_error("rt_server_release_job: job %llu is still queued or running", (unsigned long long)job_id);
+            return RT_ERR_STATE;
+        }
+        s->jobs.erase(it);
+        return RT_OK;
+    });
 }
 
 extern "C" int rt_server_wait_idle(rt_server *s, uint32_t timeout_ms) {
-    if (!s) {
-        set_error("rt_server_wait_idle: null server");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    const auto end = Clock::now() + std::chrono::milliseconds(timeout_ms);
-    for (;;) {
-        {
-            std::lock_guard<std::mutex> lk(s->mu);
-            if (s->st.completed + s->st.failed == s->st.submitted) return RT_OK;
+    return rt::guarded("rt_server_wait_idle", [&]() -> int {
+        if (!s) {
+            set_error("rt_server_wait_idle: null server");
+            return RT_ERR_INVALID_ARGUMENT;
         }
-        if (Clock::now() >= end) {
-            set_error("rt_server_wait_idle: jobs still queued or running after %u ms", timeout_ms);
-            return RT_ERR_STATE;
+        const auto end = Clock::now() + std::chrono::milliseconds(timeout_ms);
+        for (;;) {
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (s->st.completed + s->st.failed == s->st.submitted) return RT_OK;
+            }
+            if (Clock::now() >= end) {
+                set_error("rt_server_wait_idle: jobs still queued or running after %u ms", timeout_ms);
+                return RT_ERR_STATE;
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(500));
         }
-        std::this_thread::sleep_for(std::chrono::microseconds(500));
-    }
+    });
 }
 
 extern "C" int rt_server_get_stats(rt_server *s, rt_server_stats *out) {
-    if (!s || !out) {
-        set_error("rt_server_get_stats: null argument");
-        return RT_ERR_INVALID_ARGUMENT;
-    }
-    unsigned long long ctr[2] = {0, 0};
-    if (s->eng.counters.p) {
-        // a snapshot of the batch counters (kernels may be adding to them)
-        if (cudaMemcpy(ctr, s->eng.counters.p, 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
-            set_error("rt_server_get_stats: reading the counters failed");
-            return RT_ERR_CUDA;
+    return rt::guarded("rt_server_get_stats", [&]() -> int {
+        if (!s || !out) {
+            set_error("rt_server_get_stats: null argument");
+            return RT_ERR_INVALID_ARGUMENT;
         }
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    *out = s->st;
-    out->segments = ctr[0];
-    out->shadow_rays = ctr[1];
-    out->pending = (uint32_t)s->pending.size();
-    return RT_OK;
+        unsigned long long ctr[2] = {0, 0};
+        if (s->eng.counters.p) {
+            // a snapshot of the batch counters (kernels may be adding to them)
+            if (cudaMemcpy(ctr, s->eng.counters.p, 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                set_error("rt_server_get_stats: reading the counters failed");
+                return RT_ERR_CUDA;
+            }
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        *out = s->st;
+        out->segments = ctr[0];
+        out->shadow_rays = ctr[1];
+        out->pending = (uint32_t)s->pending.size();
+        return RT_OK;
+    });
 }
 
 extern "C" double rt_server_now_ms(const rt_server *s) { return s ? s->now_ms() : 0.0; }
