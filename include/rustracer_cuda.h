@@ -293,7 +293,8 @@ int rt_renderer_create_resident(rt_resident_scene *s, const rt_render_config *cf
 /* Device bytes the renderer owns now (frame, photon and path buffers; its scene not included). */
 uint64_t rt_renderer_device_bytes(const rt_renderer *r);
 /* Device bytes a renderer with this config on this scene allocates at create, and (optional) the
- * path state its first solo frame adds; for admission by footprint before creating it. */
+ * path state and job table its first solo frame adds (a photon rebuild adds the job table alone);
+ * for admission by footprint before creating it. */
 int rt_renderer_footprint(const rt_render_config *cfg, const rt_resident_scene *s, uint64_t *create_bytes,
                           uint64_t *solo_path_bytes);
 

@@ -1,7 +1,9 @@
 // The renderer behind the C ABI: device-resident scene and frame buffers, one CUDA stream, and the
 // frame schedule of rustracer-renderer's Renderer (rustracer-renderer/src/lib.rs:227-1042).
 //
-// HBM layout per renderer (all cudaMalloc'd at create, freed at destroy):
+// HBM layout per renderer (allocated at create from the device's renderer pool in the renderer's
+// stream order, freed at destroy without synchronising the device; the path state and the job table
+// come with the first solo frame):
 //   scene:  triangles 128 B, materials 64 B, lights 64 B (AoS, the reference layouts); role textures
 //           as rgba8 arrays (layer-major); the traversal layout derived from the reference's BVH:
 //           one 64 B record per internal node, one 48 B leaf-ordered triangle record per prim slot.
@@ -17,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -170,6 +173,7 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
         set_error("rt_renderer_create: cudaEventCreate failed");
         return fail(RT_ERR_CUDA);
     }
+    if (cudaMemPool_t pool = rt::renderer_pool_acquire(r->device)) r->bind_buffers(pool);
     r->cfg = *cfg;
     cudaStream_t s = r->stream;
     int st;
@@ -195,10 +199,6 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
             return fail(RT_ERR_OUT_OF_MEMORY);
         }
         RT_CK(cudaMemsetAsync(b->p, 0, npix * 16, s));
-    }
-    if (r->jobs.init(1) != cudaSuccess) {
-        set_error("rt_renderer_create: cannot allocate the job table");
-        return fail(RT_ERR_OUT_OF_MEMORY);
     }
     r->num_sms = rtd::device_sm_count();
     rtd::prepare_kernels();
@@ -242,12 +242,37 @@ int create_on(rt_resident_scene *res, const rt_render_config *cfg, rt_renderer *
 
 rt_renderer::~rt_renderer() {
     if (stream) {
+        // The frees are ordered after the renderer's own work, and a batch frame the renderer took
+        // part in is part of it (the batch makes each member's stream wait for the frame).
+        release_buffers();
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);
     }
     for (cudaEvent_t e : prof_ev)
         if (e) cudaEventDestroy(e);
     if (res) rt::resident_scene_release(res);
+    if (pooled) rt::renderer_pool_release(device);
+}
+
+void rt_renderer::bind_buffers(cudaMemPool_t pool) {
+    rt::DevBuf *b[] = {&d_lights,   &d_frame,   &d_pingpong, &d_moments,      &d_gbuffer,      &d_accum,
+                       &d_output,   &d_photons, &d_keys,     &d_rank,         &d_order,        &d_sorted,
+                       &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
+                       &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
+                       &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
+                       &path.preq,  &path.counts};
+    for (rt::DevBuf *x : b) x->bind(pool, stream);
+    pooled = true;
+}
+
+void rt_renderer::release_buffers() {
+    rt::DevBuf *b[] = {&d_lights,   &d_frame,   &d_pingpong, &d_moments,      &d_gbuffer,      &d_accum,
+                       &d_output,   &d_photons, &d_keys,     &d_rank,         &d_order,        &d_sorted,
+                       &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
+                       &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
+                       &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
+                       &path.preq,  &path.counts};
+    for (rt::DevBuf *x : b) x->release();
 }
 
 uint64_t rt_renderer::device_bytes() const {
@@ -263,6 +288,59 @@ uint64_t rt_renderer::device_bytes() const {
 }
 
 namespace rt {
+
+namespace {
+struct PoolEntry {
+    cudaMemPool_t pool = nullptr;
+    uint32_t live = 0;
+    bool tried = false;
+};
+std::mutex g_pool_mu;
+PoolEntry g_pools[64];
+}  // namespace
+
+cudaMemPool_t renderer_pool_acquire(int device) {
+    if (device < 0 || device >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    PoolEntry &e = g_pools[device];
+    if (!e.tried) {
+        e.tried = true;
+        int supported = 0;
+        if (cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, device) == cudaSuccess &&
+            supported) {
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = device;
+            if (cudaMemPoolCreate(&e.pool, &props) == cudaSuccess) {
+                uint64_t keep = ~0ull;  // freed blocks stay in the pool until the last renderer goes
+                cudaMemPoolSetAttribute(e.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            } else {
+                e.pool = nullptr;
+            }
+        }
+        cudaGetLastError();
+    }
+    if (e.pool) e.live += 1;
+    return e.pool;
+}
+
+void renderer_pool_release(int device) {
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    PoolEntry &e = g_pools[device];
+    if (e.pool && e.live > 0 && --e.live == 0) cudaMemPoolTrimTo(e.pool, 0);
+}
+
+int ensure_job_table(rt_renderer *r) {
+    if (r->jobs.ready()) return RT_OK;
+    if (r->jobs.init(1) != cudaSuccess) {
+        set_error("rt_renderer: cannot allocate the job table");
+        return RT_ERR_OUT_OF_MEMORY;
+    }
+    return RT_OK;
+}
 
 int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
     *out = nullptr;
@@ -360,11 +438,12 @@ uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {
     // The allocations of create_on: frame buffers (5 x float4 + rgba8 per pixel), photon slots, keys,
     // ranks, slot order, sorted photons and their positions, counts / cursor / meta per cell, scan partials, grid totals,
-    // counters, the one-entry job table and the renderer's own light buffer.
+    // counters and the renderer's own light buffer (the one-entry job table comes with the first solo
+    // frame or photon rebuild).
     const uint64_t npix = (uint64_t)c.width * c.height;
     const uint64_t S = photon_slots_of(c);
     return npix * (5 * 16 + 4) + S * (64 + 64 + 16 + 4 + 4 + 4) + num_cells * 16 +
-           (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + 16 + 64 + sizeof(rtd::DevJob) +
+           (uint64_t)rtd::grid_scan_partials((uint32_t)num_cells) * 4 + 16 + 64 +
            sizeof(rt_light) * std::max<uint64_t>(n_lights, 1);
 }
 
@@ -441,7 +520,8 @@ extern "C" int rt_renderer_footprint(const rt_render_config *cfg, const rt_resid
         *create_bytes = rt::renderer_create_bytes(*cfg, gp.num_cells, res->lights.size());
         if (solo_path_bytes) {
             const uint32_t spp = cfg->spp > 1u ? cfg->spp : 1u;
-            *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg));
+            *solo_path_bytes = rt::path_state_bytes((uint64_t)cfg->width * cfg->height, spp * max_bounces(*cfg)) +
+                               sizeof(rtd::DevJob);
         }
         return RT_OK;
     });
@@ -555,6 +635,7 @@ extern "C" int rt_render_frame(rt_renderer *r) {
         RT_CK(cudaEventRecord(r->events.ev[EV_FRAME0], s));
         if (fe[3]) RT_CK(cudaEventRecord(fe[0], s));
         const rtd::DevJob job = rt::make_job(r, 0u);
+        if (int st = rt::ensure_job_table(r)) return st;
         RT_CK(r->jobs.upload(&job, 1, s));
         const rtd::WaveParams wp = r->path.params(r->jobs.device(), 1u, r->d_counters.as<unsigned long long>());
         const rtd::JobShape shape{c.width,
@@ -789,6 +870,7 @@ int rt::enqueue_photon_rebuild(rt_renderer *r) {
     }
     const rtd::PhotonWave w = rtd::photon_wave_at(r->d_sorted.p, (uint32_t)traced);
     const rtd::DevJob job = rt::make_job(r, 0u);
+    if (int st = rt::ensure_job_table(r)) return st;
     RT_CK(r->jobs.upload(&job, 1, s));
     RT_CK(cudaEventRecord(r->events.ev[EV_TRACE0], s));
     RT_CK(rtd::launch_photon_wave(tp, w, r->jobs.device(), r->num_sms, r->tuning, s));

@@ -20,23 +20,35 @@
 
 namespace rt {
 
-// One cudaMalloc'd buffer, freed with its owner.
+// One device buffer, freed with its owner.  Unbound it is cudaMalloc'd (cudaFree synchronises the
+// device); bound to a memory pool and a stream it is allocated and freed in that stream's order
+// (cudaMallocFromPoolAsync / cudaFreeAsync), so freeing it waits for nothing but the stream's own
+// work.  A bound buffer must be released before its stream is destroyed.
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
+    void bind(cudaMemPool_t pl, cudaStream_t st) {
+        pool = pl;
+        stream = st;
+    }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (pool) cudaFreeAsync(p, stream);
+            else cudaFree(p);
+        }
         p = nullptr;
         bytes = 0;
     }
     cudaError_t alloc(size_t n) {
         release();
         if (n == 0) n = 16;
-        cudaError_t e = cudaMalloc(&p, n);
+        cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, n, pool, stream) : cudaMalloc(&p, n);
         if (e == cudaSuccess) bytes = n;
         else p = nullptr;
         return e;
@@ -150,15 +162,24 @@ struct JobTable {
         for (auto e : ev)
             if (e) cudaEventDestroy(e);
     }
+    bool ready() const { return host != nullptr && dev.p != nullptr; }
+    // Allocates the table for n_jobs; after a failure a second call completes what is missing.
     cudaError_t init(size_t n_jobs) {
         cudaError_t e;
-        if ((e = cudaHostAlloc(reinterpret_cast<void **>(&host), sizeof(rtd::DevJob) * n_jobs * kSlots,
-                               cudaHostAllocDefault)) != cudaSuccess)
-            return e;
-        cap = n_jobs;
+        if (!host) {
+            if ((e = cudaHostAlloc(reinterpret_cast<void **>(&host), sizeof(rtd::DevJob) * n_jobs * kSlots,
+                                   cudaHostAllocDefault)) != cudaSuccess) {
+                host = nullptr;
+                return e;
+            }
+            cap = n_jobs;
+        }
         for (auto &x : ev)
-            if ((e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming)) != cudaSuccess) return e;
-        return dev.alloc(sizeof(rtd::DevJob) * n_jobs);
+            if (!x && (e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming)) != cudaSuccess) {
+                x = nullptr;
+                return e;
+            }
+        return dev.p ? cudaSuccess : dev.alloc(sizeof(rtd::DevJob) * cap);
     }
     cudaError_t upload(const rtd::DevJob *jobs, size_t n, cudaStream_t st) {
         cudaError_t e;
@@ -222,12 +243,25 @@ struct rt_renderer {
     std::vector<cudaEvent_t> prof_ev;
     rt::DevBuf d_work;
     rt_trace_profile prof{};
+    // Every device buffer above comes from the device's renderer pool in the renderer's stream order
+    // (bind_buffers at create; release_buffers before the stream goes).
+    bool pooled = false;
+    void bind_buffers(cudaMemPool_t pool);
+    void release_buffers();
     ~rt_renderer();
     // Device bytes this renderer owns (its resident scene not included).
     uint64_t device_bytes() const;
 };
 
 namespace rt {
+// The memory pool renderer buffers come from on `device` (created on first use; freed blocks stay in
+// it for the next renderer), null if the device has no memory pools.  renderer_pool_acquire counts a
+// live renderer; renderer_pool_release uncounts it and, with none left, returns the pool's unused
+// memory to the device.
+cudaMemPool_t renderer_pool_acquire(int device);
+void renderer_pool_release(int device);
+// The renderer's job table, allocated by the first solo frame or photon rebuild that needs it.
+int ensure_job_table(rt_renderer *r);
 // Uploads a scene description (validated by the caller); *out holds one reference.
 int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out);
 void resident_scene_release(rt_resident_scene *s);

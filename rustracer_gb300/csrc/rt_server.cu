@@ -253,7 +253,9 @@ bool admit(rt_server *s) {
     const uint64_t slots_ph = c.enable_photon_map ? std::max<uint64_t>((uint64_t)c.photon_count * RT_MAX_BOUNCES, 1) : 1;
     rt_derive_grid(e.desc.bounds_min, e.desc.bounds_max, (int)e.desc.has_bounds, c.grid_max_dim,
                    c.photon_radius_mode, (uint32_t)slots_ph, &gp, &radius);
-    const uint64_t job_bytes = rt::renderer_create_bytes(c, gp.num_cells, e.desc.light_count);
+    // (a photon rebuild adds the renderer's one-entry job table)
+    const uint64_t job_bytes = rt::renderer_create_bytes(c, gp.num_cells, e.desc.light_count) +
+                               (c.enable_photon_map ? sizeof(rtd::DevJob) : 0u);
     const uint64_t need = job_bytes + (e.res ? 0 : e.bytes);
     if (!make_room(s, need, j->req.scene_id)) {
         if (!s->active.empty() || !s->flights.empty()) return false;  // wait for running jobs to finish
