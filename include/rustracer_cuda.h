@@ -276,6 +276,9 @@ void rt_render_config_default(rt_render_config *cfg);
 /* Renderer::new (lib.rs:227-663): uploads the scene, allocates frame buffers, derives the photon
  * grid (lib.rs:416-457) and writes the derived photon_radius back into the renderer's config. */
 int rt_renderer_create(const rt_scene_desc *scene, const rt_render_config *cfg, rt_renderer **out);
+/* Waits for the renderer's own stream (which every batch frame it took part in joins) and frees its
+ * buffers into the device's renderer memory pool, without synchronising the device; the pool returns
+ * its memory to the device when the last renderer on it is destroyed. */
 void rt_renderer_destroy(rt_renderer *r);
 
 /* Resident scenes (no counterpart in the reference, where each Renderer::new uploads its own copy):
