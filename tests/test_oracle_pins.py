@@ -51,6 +51,33 @@ def test_rng_f32_can_reach_one():
     assert np.float32(np.uint32(0xFFFFFF7F)) / np.float32(4294967296.0) < 1.0
 
 
+def test_unorm8_correction_equals_ieee_division():
+    """The texel conversion c / 255 of the CUDA path (rt_device.cuh unorm8): q0 = c * r with r the
+    float nearest 1/255, then q0 + (c - 255 q0) * r with both steps fused multiply-adds.  For every
+    byte it equals the correctly rounded float32 quotient, which the reference's division gives and
+    the oracle computes.  Exact rational arithmetic stands in for the GPU's fma."""
+    from fractions import Fraction
+
+    def rnd(x: Fraction) -> np.float32:  # correctly rounded, ties to even
+        f = np.float32(float(x))
+        best = None
+        for c in (np.nextafter(f, np.float32(-np.inf)), f, np.nextafter(f, np.float32(np.inf))):
+            d = abs(Fraction(float(c)) - x)
+            if best is None or d < best[0] or (d == best[0] and int(np.float32(c).view(np.uint32)) % 2 == 0):
+                best = (d, np.float32(c))
+        return best[1]
+
+    r = np.float32(float.fromhex("0x1.010102p-8"))
+    assert r == rnd(Fraction(1, 255))
+    F = lambda v: Fraction(float(v))  # noqa: E731
+    for c in range(256):
+        a = np.float32(c)
+        q0 = rnd(F(a) * F(r))
+        e = rnd(F(-q0) * 255 + F(a))
+        q = rnd(F(e) * F(r) + F(q0))
+        assert q == a / np.float32(255.0) == rnd(Fraction(c, 255)), c
+
+
 def test_fixed_sincos_error_bound(orc):
     """The sampling angles' sin / cos (one fixed IEEE sequence on both backends) against float64.
 
