@@ -547,7 +547,11 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
         const f3 ro = st.ro, inv = st.inv;
         float key[4];
         uint32_t ref[4];
-        uint32_t lr[4] = {0u, 0u, 0u, 0u}, ls[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+        // The hit leaves go straight to the lane's leaf slots (first prim slot, start of its tests in
+        // the lane's run); unused slots keep start 0xFFFFFFFF.  The previous step's readers are done
+        // (each leaf round ends at a warp barrier).
+        uint32_t *lr = &w.leaf_ref[lane].x, *ls = &w.leaf_start[lane].x;
+        w.leaf_start[lane] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
         uint32_t n_leaf = 0u;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -559,19 +563,11 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
             ref[c] = cref;
             key[c] = (hit && cnt == 0u) ? te : __int_as_float(0x7F800000);  // +inf: not a pending child
             if (hit && cnt != 0u) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if ((uint32_t)i == n_leaf) {
-                        lr[i] = cref;
-                        ls[i] = n;
-                    }
+                lr[n_leaf] = cref;
+                ls[n_leaf] = n;
                 n_leaf += 1u;
                 n += cnt;
             }
-        }
-        if (n != 0u) {
-            w.leaf_ref[lane] = make_uint4(lr[0], lr[1], lr[2], lr[3]);
-            w.leaf_start[lane] = make_uint4(ls[0], ls[1], ls[2], ls[3]);
         }
         // Near-first order of the hit internal children (a fixed five-exchange network).
         auto cswap = [&](int i, int j) {
