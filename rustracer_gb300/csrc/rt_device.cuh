@@ -385,6 +385,7 @@ __device__ __forceinline__ void warp_leaves_set_ray(WarpLeaves &w, const TravSta
 template <typename TriOf>
 __device__ __forceinline__ bool warp_leaf_rounds(TravState &st, uint32_t n, WarpLeaves &w, TriOf tri_of) {
     const uint32_t lane = threadIdx.x & 31u;
+    if (!__any_sync(0xFFFFFFFFu, n != 0u)) return false;  // no lane reached a leaf this step
     uint32_t incl = n;
 #pragma unroll
     for (uint32_t d = 1u; d < 32u; d <<= 1) {
