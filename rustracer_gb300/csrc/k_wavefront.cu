@@ -352,12 +352,7 @@ __device__ __forceinline__ uint32_t shade_key(const WaveParams &p, const uint32_
     slot = 0u;
     if (i >= n) return 4u;
     slot = q[i];
-    const float2 h = p.hit[slot];
-    if (h.x >= kInf) return 0u;
-    const DevScene &s = p.jobs[__float_as_uint(p.thr[slot].w)].scene;
-    const uint32_t mid = __float_as_uint(__ldg(s.tris + 8ull * clampi_u(__float_as_uint(h.y), s.tri_count) + 7).z);
-    const uint32_t kind = __float_as_uint(__ldg(s.mats + 4ull * clampi_u(mid, s.mat_count) + 2).z);
-    return kind == 2u ? 1u : (kind == 1u ? 3u : 2u);
+    return p.hkey[slot];  // written by the traversal with the hit
 }
 
 // kBlocks: resident blocks per SM the register allocation aims at (4: ~123 registers; 5: 96
@@ -847,7 +842,10 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                 any_hit = false;
                 st = trav_begin<kWide>(sc, xyz(o), xyz(d), kInf, (uint32_t)kStack);
                 has = sc.cnode_count != 0u;
-                if (!has) p.hit[id] = make_float2(kInf, 0.0f);
+                if (!has) {
+                    p.hit[id] = make_float2(kInf, 0.0f);
+                    p.hkey[id] = 0u;
+                }
             } else {
                 id = item - n_ext;
                 const float4 o = p.shadow[3ull * id], d = p.shadow[3ull * id + 1];
@@ -873,7 +871,10 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                                         kTree > 0 ? tree : nullptr, tree_src, tree_n)
                       : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
-                else p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
+                else {
+                    p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
+                    p.hkey[id] = (uint8_t)trav_hit_key(st);
+                }
                 has = false;
             }
             if (kCount && visiting) {

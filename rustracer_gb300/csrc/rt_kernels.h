@@ -35,6 +35,7 @@ struct WaveParams {
     float4 *rd;        // direction, .w = sample index | segment index << 16
     float4 *thr;       // throughput, .w = job index
     float2 *hit;       // closest t, primitive
+    uint8_t *hkey;     // the shade order key of the hit (0 miss, 1 dielectric, 2 Lambertian / emissive, 3 metal)
     float4 *acc;       // 4 per slot: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
     float4 *nrm;       // first-hit shading normal
     uint32_t *queue[2];
