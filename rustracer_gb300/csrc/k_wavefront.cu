@@ -352,7 +352,7 @@ __device__ __forceinline__ uint32_t shade_key(const WaveParams &p, const uint32_
     slot = 0u;
     if (i >= n) return 4u;
     slot = q[i];
-    return p.hkey[slot];  // written by the traversal with the hit
+    return p.hkey[slot] & 3u;  // written by the traversal with the hit
 }
 
 // kBlocks: resident blocks per SM the register allocation aims at (4: ~123 registers; 5: 96
@@ -424,6 +424,7 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
             const uint32_t pix = slot - job.base;
             const uint32_t px = pix % W, py = pix / W;
             const float2 h2 = p.hit[slot];
+            const uint32_t hmat = p.hkey[slot] >> 2;  // the hit's material, known before its triangle
             f3 ro = xyz(o4), rd = xyz(d4), thr = xyz(t4);
             Rng rng{__float_as_uint(o4.w)};
             const uint32_t sb = __float_as_uint(d4.w);
@@ -444,7 +445,9 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
                 alive = false;
             } else {
                 const TriFull tr = load_tri(s, prim);
-                const Mat mat = load_mat(s, tr.material_id);
+                Mat mat;
+                if (hmat != kNoMat) mat = load_mat(s, hmat);
+                else mat = load_mat(s, tr.material_id);
                 const f3 hp = ro + rd * hit_t;
                 const Bary bb = barycentric(tr, ro, rd, hit_t);
                 const float uvx = bb.uvx, uvy = bb.uvy;
@@ -873,7 +876,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                 if (occlusion) shadow_resolve(p, id, st, limit);
                 else {
                     p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
-                    p.hkey[id] = (uint8_t)trav_hit_key(st);
+                    p.hkey[id] = trav_hit_key(st);
                 }
                 has = false;
             }

@@ -373,13 +373,16 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
     if (!rt::build_traversal_layout(sd->bvh_nodes, sd->bvh_node_count, sd->bvh_prims, sd->bvh_prim_count,
                                     sd->triangles, sd->triangle_count, lay))
         return fail(RT_ERR_INVALID_ARGUMENT);
-    // Each prim slot's shade order key in its record's spare word (the first edge's .w), so the
-    // traversal can hand it to shade with the hit: 1 dielectric, 2 Lambertian or emissive, 3 metal.
+    // Each prim slot's shade order key and material (clamped as the kernels clamp it) in its record's
+    // spare word (the first edge's .w), so the traversal hands both to shade with the hit: key 1
+    // dielectric, 2 Lambertian or emissive, 3 metal.
     for (uint64_t k = 0; k < sd->bvh_prim_count; ++k) {
-        const uint32_t mid = sd->triangles[sd->bvh_prims[k]].material_id;
-        const uint32_t kind = sd->material_count ? sd->materials[std::min<uint64_t>(mid, sd->material_count - 1)].kind : 0u;
+        const uint64_t mid = std::min<uint64_t>(sd->triangles[sd->bvh_prims[k]].material_id,
+                                                sd->material_count ? sd->material_count - 1 : 0);
+        const uint32_t kind = sd->material_count ? sd->materials[mid].kind : 0u;
         const uint32_t key = kind == 2u ? 1u : (kind == 1u ? 3u : 2u);
-        std::memcpy(&lay.tri_ord[k * 12 + 7], &key, 4);
+        const uint32_t word = key | ((mid < rtd::kNoMat ? (uint32_t)mid : rtd::kNoMat) << 2);
+        std::memcpy(&lay.tri_ord[k * 12 + 7], &word, 4);
     }
     if ((st = upload(res->d_cnodes, lay.cnodes.data(), lay.cnodes.size(), s)) != RT_OK) return fail(st);
     // The four-wide records when the library traverses four-wide and a walk of them fits the largest
@@ -440,7 +443,7 @@ void resident_scene_release(rt_resident_scene *s) {
 }
 
 uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
-    return slots * 241u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
+    return slots * 244u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
 }
 
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {
