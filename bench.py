@@ -435,13 +435,14 @@ def job_objects(spec: dict, pool):
 
 
 def frame_launches(cfgs) -> int:
-    """Kernel launches of one batch frame over jobs with these configs: generate + finalize per job,
-    per iteration one trace launch (closest-hit rays of the iteration with the occlusion rays of the
-    one before), one shade and, when a job has a photon map, one photon-lookup launch; the closing
-    trace launch, the counter kernel, then per job the denoise passes and the resolve."""
+    """Kernel launches of one batch frame over jobs with these configs: one generate and one finalize
+    launch over all jobs, per iteration one trace launch (closest-hit rays of the iteration with the
+    occlusion rays of the one before), one shade and, when a job has a photon map, one photon-lookup
+    launch; the closing trace launch, the counter kernel, then per job the denoise passes and the
+    resolve."""
     iters = max(max(c.spp, 1) * (c.max_bounces or 6) for c in cfgs)
     per_iter = 3 if any(c.enable_photon_map for c in cfgs) else 2
-    return (2 * len(cfgs) + per_iter * iters + 2 +
+    return (2 + per_iter * iters + 2 +
             sum((c.denoise_passes or 2) * int(c.enable_denoise) + 1 for c in cfgs))
 
 

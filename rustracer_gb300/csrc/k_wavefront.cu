@@ -216,15 +216,32 @@ __device__ __forceinline__ uint32_t pack_sb(uint32_t s, uint32_t b) { return (s 
 
 }  // namespace
 
+// The last job whose first index (`first` of DevJob: base slot or first tile) is at or below i; jobs
+// are laid out in order, so their first indices ascend.
+template <typename First>
+__device__ __forceinline__ uint32_t job_of(const WaveParams &p, uint32_t i, First first) {
+    uint32_t lo = 0u, hi = p.n_jobs;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (first(p.jobs[mid]) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // ------------------------------------------------------------------------------------------------
-// generate: 8 x 4 pixel tiles, one per warp, so the first queue is tile-coherent.  One launch per job.
+// generate: 8 x 4 pixel tiles, one per warp, so the first queue is tile-coherent.  One launch over
+// every job's tiles (job j's start at its tile0).
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant__ WaveParams p, uint32_t jid) {
+__global__ void __launch_bounds__(128) wf_generate_kernel(const __grid_constant__ WaveParams p, uint32_t n_tiles) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t gtile = blockIdx.x * 4u + warp;
+    if (gtile >= n_tiles) return;  // whole warps: warp_append below is warp-uniform
+    const uint32_t jid = job_of(p, gtile, [](const DevJob &j) { return j.tile0; });
     const DevJob &job = p.jobs[jid];
     const uint32_t W = job.ip.width, H = job.ip.height;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t tiles_x = (W + 7u) / 8u;
-    const uint32_t tile = blockIdx.x * 4u + warp;
+    const uint32_t tile = gtile - job.tile0;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     const uint32_t px = tx * 8u + (lane & 7u), py = ty * 4u + (lane >> 3);
     const bool active = px < W && py < H;
@@ -902,13 +919,15 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
 }
 
 // ------------------------------------------------------------------------------------------------
-// finalize: firefly sigma clamp and the frame outputs (gather.wgsl:548-593).  One launch per job.
+// finalize: firefly sigma clamp and the frame outputs (gather.wgsl:548-593).  One launch over every
+// job's slots.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant__ WaveParams p, uint32_t jid) {
-    const DevJob &job = p.jobs[jid];
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) wf_finalize_kernel(const __grid_constant__ WaveParams p, uint32_t n_slots) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n_slots) return;
+    const DevJob &job = p.jobs[job_of(p, slot, [](const DevJob &j) { return j.base; })];
+    const uint32_t pix = slot - job.base;
     if (pix >= job.npix) return;
-    const uint32_t slot = job.base + pix;
     const uint32_t spp = job.spp;
     Accum A = load_acc(p, slot);
     const float first_depth = p.acc[4 * (size_t)slot + 1].y;
@@ -1085,14 +1104,15 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
     uint64_t slots = 0;
     uint32_t stack_need = 0, wide_need = 0;
     bool wide = n_jobs > 0;  // four-wide records when every job's scene has them
+    uint64_t tiles = 0;
     for (uint32_t j = 0; j < n_jobs; ++j) {
-        const uint32_t tiles = ((jobs[j].width + 7u) / 8u) * ((jobs[j].height + 3u) / 4u);
-        wf_generate_kernel<<<(tiles + 3u) / 4u, 128, 0, st>>>(p, j);
+        tiles += ((jobs[j].width + 7u) / 8u) * ((jobs[j].height + 3u) / 4u);
         slots += jobs[j].npix;
         stack_need = jobs[j].stack_cap > stack_need ? jobs[j].stack_cap : stack_need;
         wide_need = jobs[j].wide_stack > wide_need ? jobs[j].wide_stack : wide_need;
         wide = wide && jobs[j].wide != 0u;
     }
+    if (tiles) wf_generate_kernel<<<(unsigned)((tiles + 3u) / 4u), 128, 0, st>>>(p, (uint32_t)tiles);
     WaveTuning t = tune;
     normalize_tuning(t, wide ? wide_need : stack_need);
     ExtendKernel ext;
@@ -1153,7 +1173,7 @@ cudaError_t launch_wavefront(const WaveParams &p, const JobShape *jobs, uint32_t
         prof->shade_launches = n_shd;
         prof->photon_launches = n_pho;
     }
-    for (uint32_t j = 0; j < n_jobs; ++j) wf_finalize_kernel<<<(jobs[j].npix + 255u) / 256u, 256, 0, st>>>(p, j);
+    if (slots) wf_finalize_kernel<<<(unsigned)((slots + 255u) / 256u), 256, 0, st>>>(p, (uint32_t)slots);
     wf_count_kernel<<<1, 32, 0, st>>>(p, iters);
     return cudaGetLastError();
 }

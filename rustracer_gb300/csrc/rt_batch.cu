@@ -142,9 +142,12 @@ int BatchEngine::frame(rt_renderer *const *rs, uint32_t n) {
         return RT_ERR_INVALID_ARGUMENT;
     }
     if (int st = reserve(slots, iters)) return st;
+    uint32_t tile0 = 0;
     for (uint32_t j = 0; j < n; ++j) {
         alpha[j] = rt::prepare_frame(rs[j]);
         table[j] = rt::make_job(rs[j], base[j]);
+        table[j].tile0 = tile0;  // the job's first tile in the frame's one generate launch
+        tile0 += ((rs[j]->cfg.width + 7u) / 8u) * ((rs[j]->cfg.height + 3u) / 4u);
     }
     cudaEvent_t fe[2] = {nullptr, nullptr};
     for (auto &e : fe) RT_CK(ring.next(&e));

@@ -20,6 +20,7 @@ struct DevJob {
     uint64_t sorted_count;
     const uint2 *grid_meta;        // (start, count) per cell
     uint32_t max_bounces, npix, base, spp;  // base: first path slot; spp = max(1, ip.spp)
+    uint32_t tile0, tile_pad;               // first 8 x 4 tile of the job in the frame's generate launch
     float4 *frame;
     float4 *moments;
     float4 *gbuffer;
