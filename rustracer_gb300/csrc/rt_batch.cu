@@ -36,16 +36,28 @@ BatchEngine::~BatchEngine() {
     if (stream) cudaStreamSynchronize(stream);
     if (exec) cudaGraphExecDestroy(exec);
     if (done) cudaEventDestroy(done);
+    if (fork) cudaEventDestroy(fork);
+    for (int i = 0; i < kSide; ++i) {
+        if (join[i]) cudaEventDestroy(join[i]);
+        if (side[i]) cudaStreamDestroy(side[i]);
+    }
     if (stream) cudaStreamDestroy(stream);
 }
 
 int BatchEngine::init(uint32_t max_jobs, GraphMode mode) {
     graph_mode = mode;
     if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) {
         set_error("batch: cannot create the stream");
         return RT_ERR_CUDA;
     }
+    for (int i = 0; i < kSide; ++i)
+        if (cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming) != cudaSuccess) {
+            set_error("batch: cannot create the side streams");
+            return RT_ERR_CUDA;
+        }
     if (jobs.init(max_jobs) != cudaSuccess || counters.alloc(64) != cudaSuccess ||
         cudaMemset(counters.p, 0, 64) != cudaSuccess) {
         set_error("batch: out of device memory for the job table");
@@ -110,10 +122,18 @@ int BatchEngine::enqueue(rt_renderer *const *rs, uint32_t n, uint32_t iters, con
     }
     const rtd::WaveParams wp = path.params(jobs.device(), n, counters.as<unsigned long long>());
     RT_CK(rtd::launch_wavefront(wp, shapes.data(), n, iters, num_sms, tuning, stream));
-    for (uint32_t j = 0; j < n; ++j)
-        if (int st = rt::enqueue_post(rs[j], alpha[j], dev_alpha ? &jobs.device()[j].alpha : nullptr, stream))
-            return st;
-    return RT_OK;
+    // Each member's denoise and resolve on one of the side streams, joined back before the frame ends.
+    const int k = n < (uint32_t)kSide ? (int)n : kSide;
+    RT_CK(cudaEventRecord(fork, stream));
+    for (int i = 0; i < k; ++i) RT_CK(cudaStreamWaitEvent(side[i], fork, 0));
+    int st = RT_OK;
+    for (uint32_t j = 0; j < n && st == RT_OK; ++j)
+        st = rt::enqueue_post(rs[j], alpha[j], dev_alpha ? &jobs.device()[j].alpha : nullptr, side[j % k]);
+    for (int i = 0; i < k; ++i) {  // joined even after a failure, so a capture can end
+        RT_CK(cudaEventRecord(join[i], side[i]));
+        RT_CK(cudaStreamWaitEvent(stream, join[i], 0));
+    }
+    return st;
 }
 
 int BatchEngine::frame(rt_renderer *const *rs, uint32_t n) {

@@ -30,6 +30,11 @@ struct BatchEngine {
     uint64_t frames = 0, captures = 0;
     cudaEvent_t done = nullptr;
     FrameEventRing ring;  // two events per frame (start, end)
+    // Side streams for the members' denoise and resolve, which touch only each member's own buffers:
+    // forked from and joined back to `stream` (parallel branches of a captured frame).
+    static constexpr int kSide = 4;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork = nullptr, join[kSide] = {};
 
     ~BatchEngine();
     int init(uint32_t max_jobs, GraphMode mode);
