@@ -189,3 +189,31 @@ def test_treelet_in_a_batch_of_several_scenes(gpu, specs, alone):
     for j, r in enumerate(rs):
         assert same(outputs(r), alone[j][0]), f"job {j}"
     b.close()
+
+
+def test_renderer_buffers_are_reused(gpu):
+    """A renderer's buffers come from the device's renderer pool in its stream order: destroying one
+    and creating another of the same shape reuses the freed blocks, so repeated create / render /
+    destroy cycles leave free device memory where the first cycle left it (no growth, no leak)."""
+    torch = pytest.importorskip("torch")
+    scene = rt.Scene.cornell555()
+    cfg = rt.RenderConfig(width=640, height=480, spp=1, accumulate_frames=4, enable_denoise=True,
+                          enable_photon_map=True, photon_count=1 << 16)
+
+    def cycle():
+        r = rt.Renderer(scene, cfg)
+        r.update_camera(scene.default_camera())
+        r.rebuild_photons()
+        r.render_frames(2)
+        acc = r.read_accumulation()
+        r.close()
+        torch.cuda.synchronize()
+        return acc
+
+    keep = rt.Renderer(scene, cfg)  # a live renderer keeps the pool from being trimmed in between
+    first = cycle()  # its freed buffers stay in the pool
+    free_after_first = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert np.array_equal(cycle(), first)  # the reused buffers start clean: same image
+        assert abs(torch.cuda.mem_get_info()[0] - free_after_first) <= 8 << 20
+    keep.close()
