@@ -102,3 +102,33 @@ def test_real_photographs(lib):
         assert 20 < rgb.mean() < 235 and rgb.std() > 20
         # neighbouring pixels of a photograph are close on average (a decoding error breaks this)
         assert np.abs(np.diff(rgb, axis=1)).mean() < 20
+
+
+def test_corrupted_streams_fail_cleanly(lib):
+    """Seeded corruptions of valid baseline and progressive files (flipped bytes, truncations, spliced
+    segments): every call returns an image or a refusal with a message; none crashes or hangs."""
+    rng = np.random.default_rng(11)
+    img = image(40, 56, seed=5)
+    sources = [encode_baseline(img, Q_COARSE, subsample=True, restart=2),
+               encode_progressive(img, Q_COARSE, subsample=True, approx=True)]
+    decoded = refused = 0
+    for src in sources:
+        for trial in range(150):
+            b = bytearray(src)
+            kind = trial % 3
+            if kind == 0:
+                for _ in range(int(rng.integers(1, 8))):
+                    b[int(rng.integers(2, len(b)))] = int(rng.integers(0, 256))
+            elif kind == 1:
+                b = b[: int(rng.integers(2, len(b)))]
+            else:
+                i, j = sorted(int(x) for x in rng.integers(2, len(b), 2))
+                b = b[:i] + b[j:] + b[i:j]
+            t = gltf.decode_jpeg(bytes(b))
+            if t is None:
+                refused += 1
+                assert A.load().rt_last_error()
+            else:
+                decoded += 1
+                assert np.isfinite(np.asarray(t.data)).all()
+    assert decoded + refused == 2 * 150 and refused > 0
