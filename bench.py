@@ -271,10 +271,9 @@ def run_reference(args, w):
 # ------------------------------------------------------------------------------------------------
 # Bytes of per-ray state a traversal launch moves besides the tree: a closest-hit ray reads its
 # queue entry (4), origin and direction (32) and the job word of its throughput (16) and writes its
-# hit (8) and the hit's shade key and material word (4); an occlusion ray reads its 48-byte record
-# and, when the light is visible, adds its term to the accumulator (16 read + 16 written, counted for
-# every ray: an upper bound).
-CLOSEST_RAY_BYTES = 4 + 32 + 16 + 8 + 4
+# hit (8); an occlusion ray reads its 48-byte record and, when the light is visible, adds its term to
+# the accumulator (16 read + 16 written, counted for every ray: an upper bound).
+CLOSEST_RAY_BYTES = 4 + 32 + 16 + 8
 OCCLUSION_RAY_BYTES = 48 + 32
 TRI_BYTES = 48  # one leaf-ordered triangle record: v0 (+ index), v1 - v0, v2 - v0
 

@@ -441,7 +441,7 @@ int rt_get_tuning(const rt_renderer *r, rt_wavefront_tuning *t);
  * A job's scene is uploaded on first use and stays resident after its jobs finish; when the cap
  * would be exceeded, idle resident scenes (no admitted job) are freed least recently used first.
  * The device bytes charged against the cap are the resident scenes, the admitted jobs' renderer
- * buffers and the path state (max_slots x 244 B, reserved at create).  A job's image equals
+ * buffers and the path state (max_slots x 240 B, reserved at create).  A job's image equals
  * the image of the same request rendered alone by rt_renderer_create + rt_render_frame.
  * Registered scene descriptions are borrowed: their arrays must stay valid and unchanged until
  * rt_server_destroy.  submit / status / read_result / release / stats may be called from any thread.

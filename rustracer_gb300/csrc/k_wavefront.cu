@@ -364,12 +364,22 @@ __global__ void __launch_bounds__(kBlock) wf_extend_kernel(const __grid_constant
 // ------------------------------------------------------------------------------------------------
 constexpr uint32_t kShadeKeys = 5;  // miss, dielectric, Lambertian / emissive, metal, no entry
 
+// The entry's order key; for a hit also its triangle and material word, read from the hit prim
+// slot's record (the traversal stores the slot: `orig` = the triangle's index, `word` = key | material
+// << 2, filled at scene upload).
 __device__ __forceinline__ uint32_t shade_key(const WaveParams &p, const uint32_t *q, uint32_t i, uint32_t n,
-                                              uint32_t &slot) {
+                                              uint32_t &slot, uint32_t &orig, uint32_t &word) {
     slot = 0u;
+    orig = 0u;
+    word = 0u;
     if (i >= n) return 4u;
     slot = q[i];
-    return p.hkey[slot] & 3u;  // written by the traversal with the hit
+    const float2 h = p.hit[slot];
+    if (h.x >= kInf) return 0u;
+    const float4 *rec = p.jobs[__float_as_uint(p.thr[slot].w)].scene.tri_ord + 3ull * __float_as_uint(h.y);
+    orig = __float_as_uint(__ldg(rec).w);
+    word = __float_as_uint(__ldg(rec + 1).w);
+    return word & 3u;
 }
 
 // kBlocks: resident blocks per SM the register allocation aims at (4: ~123 registers; 5: 96
@@ -383,6 +393,7 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
     __shared__ uint8_t s_emit[128];   // by original position: 1 survives, 2 shadow ray, 4 photon lookup
     __shared__ uint32_t s_spos[128];  // by original position: shadow record index
     __shared__ uint32_t s_ppos[128];  // by original position: photon-lookup record index
+    __shared__ uint32_t s_orig[128], s_word[128];  // by shading position: the hit's triangle and material word
     const uint32_t n = p.counts[4 * iter];
     const uint32_t *q = p.queue[iter & 1u];
     uint32_t *q_next = p.queue[(iter + 1u) & 1u];
@@ -397,8 +408,8 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
         // The block's entries ranked by key, stable (warp-major, then lane order within a key).
         const uint32_t round_base = r * stride + blockIdx.x * blockDim.x;
         const uint32_t i_own = round_base + threadIdx.x;
-        uint32_t slot_own;
-        const uint32_t key = shade_key(p, q, i_own, n, slot_own);
+        uint32_t slot_own, orig_own, word_own;
+        const uint32_t key = shade_key(p, q, i_own, n, slot_own, orig_own, word_own);
         uint32_t same = 0;
 #pragma unroll
         for (uint32_t k = 0; k < kShadeKeys; ++k) {
@@ -414,6 +425,8 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
             for (uint32_t w = 0; w < 4; ++w)
                 if (k < key || (k == key && w < warp)) pos += s_count[w][k];
         s_order[pos] = i_own;
+        s_orig[pos] = orig_own;
+        s_word[pos] = word_own;
         __syncthreads();
         const uint32_t i = s_order[threadIdx.x];
         const bool valid = i < n;
@@ -441,13 +454,13 @@ __global__ void __launch_bounds__(128, kBlocks) wf_shade_kernel(const __grid_con
             const uint32_t pix = slot - job.base;
             const uint32_t px = pix % W, py = pix / W;
             const float2 h2 = p.hit[slot];
-            const uint32_t hmat = p.hkey[slot] >> 2;  // the hit's material, known before its triangle
+            const uint32_t hmat = s_word[threadIdx.x] >> 2;  // the hit's material, known before its triangle
             f3 ro = xyz(o4), rd = xyz(d4), thr = xyz(t4);
             Rng rng{__float_as_uint(o4.w)};
             const uint32_t sb = __float_as_uint(d4.w);
             uint32_t sidx = sb & 0xFFFFu, b = sb >> 16;
             const float hit_t = h2.x;
-            const uint32_t prim = __float_as_uint(h2.y);
+            const uint32_t prim = s_orig[threadIdx.x];  // the hit triangle (h2.y holds its prim slot)
             float4 *acc = p.acc + 4 * (size_t)slot;
             const uint32_t sidx0 = sidx;
             const float4 acc0 = acc[0];
@@ -862,10 +875,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                 any_hit = false;
                 st = trav_begin<kWide>(sc, xyz(o), xyz(d), kInf, (uint32_t)kStack);
                 has = sc.cnode_count != 0u;
-                if (!has) {
-                    p.hit[id] = make_float2(kInf, 0.0f);
-                    p.hkey[id] = 0u;
-                }
+                if (!has) p.hit[id] = make_float2(kInf, 0.0f);
             } else {
                 id = item - n_ext;
                 const float4 o = p.shadow[3ull * id], d = p.shadow[3ull * id + 1];
@@ -891,10 +901,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) wf_trace_kernel(const _
                                         kTree > 0 ? tree : nullptr, tree_src, tree_n)
                       : trav_step_warp(st, has, any_hit, stk, (uint32_t)kBlock, wl, kCount ? &tests : nullptr)) {
                 if (occlusion) shadow_resolve(p, id, st, limit);
-                else {
-                    p.hit[id] = make_float2(st.t, __uint_as_float(trav_hit_prim(st)));
-                    p.hkey[id] = trav_hit_key(st);
-                }
+                else p.hit[id] = make_float2(st.t, __uint_as_float(st.prim));  // the hit's prim slot
                 has = false;
             }
             if (kCount && visiting) {

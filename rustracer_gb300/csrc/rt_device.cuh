@@ -622,10 +622,7 @@ __device__ __forceinline__ bool trav_step_warp4(TravState &st, bool active, bool
 __device__ __forceinline__ uint32_t trav_hit_prim(const TravState &st) {
     return st.t < kInf ? __float_as_uint(__ldg(st.tri_ord + 3ull * st.prim).w) : 0u;
 }
-// The shade order key and material word of that hit (the prim slot's record carries it; 0 for a miss).
-__device__ __forceinline__ uint32_t trav_hit_key(const TravState &st) {
-    return st.t < kInf ? __float_as_uint(__ldg(st.tri_ord + 3ull * st.prim + 1).w) : 0u;
-}
+
 
 struct Bary {
     float uvx, uvy, u, v;

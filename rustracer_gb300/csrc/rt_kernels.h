@@ -29,16 +29,14 @@ struct DevJob {
 
 // The wavefront gather pass over one or more jobs.  Path state has one slot per pixel of every job
 // (slot = job.base + pixel); queues hold slots of any job.
-constexpr uint32_t kNoMat = 0x3FFFFFFFu;  // a material index the hit key word cannot carry
+constexpr uint32_t kNoMat = 0x3FFFFFFFu;  // a material index a prim slot's key word cannot carry
 struct WaveParams {
     const DevJob *jobs;
     uint32_t n_jobs;
     float4 *ro;        // origin, .w = RNG state
     float4 *rd;        // direction, .w = sample index | segment index << 16
     float4 *thr;       // throughput, .w = job index
-    float2 *hit;       // closest t, primitive
-    uint32_t *hkey;    // the hit's shade order key (bits 0-1: 0 miss, 1 dielectric, 2 Lambertian / emissive,
-                       // 3 metal) and material (bits 2-31, clamped to the scene's; kNoMat: read the triangle's)
+    float2 *hit;       // closest t, the hit's prim slot
     float4 *acc;       // 4 per slot: (col, lum_sum), (lum2_sum, first_depth, -, -), sample_lum[0..8]
     float4 *nrm;       // first-hit shading normal
     uint32_t *queue[2];

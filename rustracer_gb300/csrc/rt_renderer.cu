@@ -260,7 +260,7 @@ void rt_renderer::bind_buffers(cudaMemPool_t pool) {
                        &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
                        &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
                        &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
-                       &path.preq,  &path.hkey, &path.counts};
+                       &path.preq,  &path.counts};
     for (rt::DevBuf *x : b) x->bind(pool, stream);
     pooled = true;
 }
@@ -271,7 +271,7 @@ void rt_renderer::release_buffers() {
                        &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
                        &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
                        &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
-                       &path.preq,  &path.hkey, &path.counts};
+                       &path.preq,  &path.counts};
     for (rt::DevBuf *x : b) x->release();
 }
 
@@ -281,9 +281,9 @@ uint64_t rt_renderer::device_bytes() const {
                  d_sorted_pos.bytes + d_rank.bytes +
                  d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
                  d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
-    const rt::DevBuf *pb[11] = {&path.ro,       &path.rd,       &path.thr,      &path.hit,    &path.acc, &path.nrm,
-                                &path.queue[0], &path.queue[1], &path.shadow, &path.preq, &path.hkey};
-    for (int i = 0; i < 11; ++i) n += pb[i]->bytes;
+    const rt::DevBuf *pb[10] = {&path.ro,       &path.rd,       &path.thr,      &path.hit,    &path.acc,
+                                &path.nrm,      &path.queue[0], &path.queue[1], &path.shadow, &path.preq};
+    for (int i = 0; i < 10; ++i) n += pb[i]->bytes;
     return n;
 }
 
@@ -374,8 +374,8 @@ int resident_scene_create(const rt_scene_desc *sd, rt_resident_scene **out) {
                                     sd->triangles, sd->triangle_count, lay))
         return fail(RT_ERR_INVALID_ARGUMENT);
     // Each prim slot's shade order key and material (clamped as the kernels clamp it) in its record's
-    // spare word (the first edge's .w), so the traversal hands both to shade with the hit: key 1
-    // dielectric, 2 Lambertian or emissive, 3 metal.
+    // spare word (the first edge's .w), which shade reads with the hit's prim slot: key 1 dielectric,
+    // 2 Lambertian or emissive, 3 metal.
     for (uint64_t k = 0; k < sd->bvh_prim_count; ++k) {
         const uint64_t mid = std::min<uint64_t>(sd->triangles[sd->bvh_prims[k]].material_id,
                                                 sd->material_count ? sd->material_count - 1 : 0);
@@ -443,7 +443,7 @@ void resident_scene_release(rt_resident_scene *s) {
 }
 
 uint64_t path_state_bytes(uint64_t slots, uint32_t iters) {
-    return slots * 244u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
+    return slots * 240u + sizeof(uint32_t) * 4ull * ((uint64_t)iters + 1);
 }
 
 uint64_t renderer_create_bytes(const rt_render_config &c, uint64_t num_cells, uint64_t n_lights) {

@@ -99,17 +99,17 @@ struct FrameEventRing {
     }
 };
 
-// Wavefront path state for `slots` pixel slots (244 B per slot) and the per-iteration counters.
+// Wavefront path state for `slots` pixel slots (240 B per slot) and the per-iteration counters.
 struct PathState {
-    DevBuf ro, rd, thr, hit, acc, nrm, queue[2], shadow, preq, hkey, counts;
+    DevBuf ro, rd, thr, hit, acc, nrm, queue[2], shadow, preq, counts;
     size_t slots = 0, counts_bytes = 0;
     // (Re)allocates when too small.  The caller's stream must be idle.
     cudaError_t ensure(size_t n_slots, uint32_t iters) {
         cudaError_t e;
         if (n_slots > slots) {
-            DevBuf *b[11] = {&ro, &rd, &thr, &nrm, &hit, &acc, &queue[0], &queue[1], &shadow, &preq, &hkey};
-            const size_t sz[11] = {16, 16, 16, 16, 8, 64, 4, 4, 48, 48, 4};
-            for (int i = 0; i < 11; ++i)
+            DevBuf *b[10] = {&ro, &rd, &thr, &nrm, &hit, &acc, &queue[0], &queue[1], &shadow, &preq};
+            const size_t sz[10] = {16, 16, 16, 16, 8, 64, 4, 4, 48, 48};
+            for (int i = 0; i < 10; ++i)
                 if ((e = b[i]->alloc(n_slots * sz[i])) != cudaSuccess) {
                     slots = 0;
                     return e;
@@ -135,7 +135,6 @@ struct PathState {
         w.rd = rd.as<float4>();
         w.thr = thr.as<float4>();
         w.hit = hit.as<float2>();
-        w.hkey = hkey.as<uint32_t>();
         w.acc = acc.as<float4>();
         w.nrm = nrm.as<float4>();
         w.queue[0] = queue[0].as<uint32_t>();
