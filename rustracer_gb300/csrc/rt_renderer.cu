@@ -254,36 +254,26 @@ rt_renderer::~rt_renderer() {
     if (pooled) rt::renderer_pool_release(device);
 }
 
+std::array<rt::DevBuf *, 32> rt_renderer::buffers() {
+    return {&d_lights,   &d_frame,   &d_pingpong, &d_moments,     &d_gbuffer,     &d_accum,       &d_output,
+            &d_photons,  &d_keys,    &d_rank,     &d_order,       &d_sorted,      &d_sorted_pos,  &d_counts,
+            &d_meta,     &d_cursor,  &d_partials, &d_total,       &d_counters,    &d_work,        &jobs.dev,
+            &path.ro,    &path.rd,   &path.thr,   &path.hit,      &path.acc,      &path.nrm,      &path.queue[0],
+            &path.queue[1], &path.shadow, &path.preq, &path.counts};
+}
+
 void rt_renderer::bind_buffers(cudaMemPool_t pool) {
-    rt::DevBuf *b[] = {&d_lights,   &d_frame,   &d_pingpong, &d_moments,      &d_gbuffer,      &d_accum,
-                       &d_output,   &d_photons, &d_keys,     &d_rank,         &d_order,        &d_sorted,
-                       &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
-                       &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
-                       &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
-                       &path.preq,  &path.counts};
-    for (rt::DevBuf *x : b) x->bind(pool, stream);
+    for (rt::DevBuf *b : buffers()) b->bind(pool, stream);
     pooled = true;
 }
 
 void rt_renderer::release_buffers() {
-    rt::DevBuf *b[] = {&d_lights,   &d_frame,   &d_pingpong, &d_moments,      &d_gbuffer,      &d_accum,
-                       &d_output,   &d_photons, &d_keys,     &d_rank,         &d_order,        &d_sorted,
-                       &d_sorted_pos, &d_counts, &d_meta,    &d_cursor,       &d_partials,     &d_total,
-                       &d_counters, &d_work,    &jobs.dev,   &path.ro,        &path.rd,        &path.thr,
-                       &path.hit,   &path.acc,  &path.nrm,   &path.queue[0],  &path.queue[1],  &path.shadow,
-                       &path.preq,  &path.counts};
-    for (rt::DevBuf *x : b) x->release();
+    for (rt::DevBuf *b : buffers()) b->release();
 }
 
 uint64_t rt_renderer::device_bytes() const {
-    uint64_t n = d_lights.bytes + d_frame.bytes + d_pingpong.bytes + d_moments.bytes + d_gbuffer.bytes +
-                 d_accum.bytes + d_output.bytes + d_photons.bytes + d_keys.bytes + d_order.bytes + d_sorted.bytes +
-                 d_sorted_pos.bytes + d_rank.bytes +
-                 d_counts.bytes + d_meta.bytes + d_cursor.bytes + d_partials.bytes + d_total.bytes +
-                 d_counters.bytes + jobs.dev.bytes + path.counts.bytes;
-    const rt::DevBuf *pb[10] = {&path.ro,       &path.rd,       &path.thr,      &path.hit,    &path.acc,
-                                &path.nrm,      &path.queue[0], &path.queue[1], &path.shadow, &path.preq};
-    for (int i = 0; i < 10; ++i) n += pb[i]->bytes;
+    uint64_t n = 0;
+    for (const rt::DevBuf *b : const_cast<rt_renderer *>(this)->buffers()) n += b->bytes;
     return n;
 }
 

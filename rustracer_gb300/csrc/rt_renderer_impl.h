@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cstring>
 #include <vector>
@@ -246,6 +247,7 @@ struct rt_renderer {
     // Every device buffer above comes from the device's renderer pool in the renderer's stream order
     // (bind_buffers at create; release_buffers before the stream goes).
     bool pooled = false;
+    std::array<rt::DevBuf *, 32> buffers();  // every device buffer the renderer owns
     void bind_buffers(cudaMemPool_t pool);
     void release_buffers();
     ~rt_renderer();
